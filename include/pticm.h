@@ -1,0 +1,184 @@
+/*
+ * pticm.h -- C ABI of the GB300 (sm_103a) PT-ICM engine.
+ *
+ * Parallel tempering with isoenergetic cluster moves for Ising spin glasses
+ * and MaxCut on Gset graphs.  Every replica of a run is resident on one GPU;
+ * one persistent kernel performs, per PT step, colour-class Metropolis
+ * sweeps, replica exchange as a permutation of temperature slots, and
+ * union-find cluster moves.
+ *
+ * Conventions: every function returns a pticm_status (0 = success); no
+ * exceptions cross this boundary; pticm_last_error() describes the last
+ * failure of the calling thread.  Buffers passed in are plain host memory and
+ * are copied.  Spin states at this boundary are one byte per site, 0 or 1 in
+ * the reference's bool convention (true = +1), in the ORIGINAL site order of
+ * the problem file.  Energies follow the reference's sign convention
+ * E = sum_i h_i s_i + sum_{i<j} J_ij s_i s_j.
+ *
+ * Each declaration cites the reference interface it replaces
+ * (mxburns2022/PT-ICM, paths relative to that project).
+ */
+#ifndef PTICM_H
+#define PTICM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pticm_status {
+    PTICM_OK = 0,
+    PTICM_ERR_INVALID = 1,      /* bad argument or call order                  */
+    PTICM_ERR_IO = 2,           /* unreadable or malformed problem file        */
+    PTICM_ERR_UNSUPPORTED = 3,  /* e.g. non-integer couplings, self loops      */
+    PTICM_ERR_CUDA = 4,         /* CUDA runtime failure                        */
+    PTICM_ERR_DEVICE = 5,       /* a kernel reported a failure (bounded wait,  */
+                                /* replay mismatch, bounds check)              */
+    PTICM_ERR_NOMEM = 6,        /* host or device allocation failed            */
+    PTICM_ERR_NODEVICE = 7      /* no CUDA device (the engine has no CPU path) */
+} pticm_status;
+
+typedef struct pticm_problem pticm_problem;
+typedef struct pticm_ctx pticm_ctx;
+
+/* ------------------------------------------------------------ problems -- */
+typedef struct pticm_problem_info {
+    int64_t n;              /* spins                                          */
+    int64_t m;              /* edges as counted in the file header            */
+    int64_t nnz;            /* directed adjacency entries                     */
+    int32_t sparse;         /* reference's sparse/dense choice (density<10%)  */
+    int32_t ncolors;        /* colour classes of the sweep order              */
+    int32_t kmax;           /* largest |dE|/2                                 */
+    int32_t has_linear;     /* nonzero linear terms                           */
+    double char_scale;      /* max(mean w, var w): ICM temperature cutoff     */
+    double total_weight;    /* sum of edge weights (cut = (W - E_J)/2)        */
+} pticm_problem_info;
+
+/* Problem(path, seed, burn_in)  src/problem.cc:183-247.  Honours the
+ * reference's rules: ".gset"/".ising" anywhere in the path means 0-based
+ * vertices, else 1-based; a missing weight is 1; ".ising" files carry a
+ * linear-term block.  Couplings and linear terms must be integers in
+ * [-127, 127] (PTICM_ERR_UNSUPPORTED otherwise). */
+int pticm_problem_load_gset(const char* path, pticm_problem** out);
+
+/* Problem(weights, src, dest, linear, seed, burn_in, N, M)
+ * include/problem.hh:43-62.  `h` may be NULL. */
+int pticm_problem_from_coo(int64_t n, int64_t m, const int32_t* src, const int32_t* dst,
+                           const double* w, const double* h, pticm_problem** out);
+
+/* Problem(formulation, linear, seed, burn_in, N)  include/problem.hh:23-42:
+ * a dense row-major n*n coupling matrix (only j != i entries are used; zero
+ * entries are not edges).  `h` may be NULL. */
+int pticm_problem_from_dense(int64_t n, const double* J, const double* h, pticm_problem** out);
+
+void pticm_problem_free(pticm_problem* p);
+int pticm_problem_get_info(const pticm_problem* p, pticm_problem_info* out);
+
+/* Problem::energy, Problem::maxcut, Problem::calculate_dE
+ * src/problem.cc:33-162, computed on the GPU for `count` states
+ * (count*n bytes).  `dE` (count*n doubles) may be NULL. */
+int pticm_problem_evaluate(const pticm_problem* p, int64_t count, const uint8_t* states,
+                           double* energy, double* maxcut, double* dE);
+
+/* --------------------------------------------------------- PT contexts -- */
+typedef struct pticm_opts {
+    uint64_t seed;          /* -s                                             */
+    uint32_t nt;            /* -r: temperatures per chain                     */
+    uint32_t chains;        /* replicas per temperature (2 in the reference)  */
+    uint32_t sweeps;        /* --sweeps per PT step                           */
+    uint32_t icm;           /* --icm                                          */
+    uint32_t exchange;      /* 0 reference attempt order, 1 even/odd rounds   */
+    uint32_t best_per_phase;/* 1: best state checked after every colour class */
+    uint32_t block_threads; /* 0 = automatic                                  */
+    uint32_t replicas_per_block; /* 0 = automatic                             */
+} pticm_opts;
+
+void pticm_opts_default(pticm_opts* o);
+
+/* State of solve() between initialisation and reporting
+ * (src/solver.cc:16-166, include/mpi_defs.hh:33-65): all replicas of the
+ * problem resident on the current CUDA device. */
+int pticm_create(const pticm_problem* p, const pticm_opts* o, pticm_ctx** out);
+void pticm_destroy(pticm_ctx* c);
+
+/* initialize_temperatures (src/initialization.cc:103-191) with an explicit
+ * ladder of nt inverse temperatures (slot k of every chain gets beta[k]).
+ * The ICM pair count follows src/initialization.cc:158-164 (entries from the
+ * top slot down while beta >= char_scale) unless `nc` >= 0 sets it. */
+int pticm_set_ladder(pticm_ctx* c, const double* beta, uint32_t nt, int32_t nc);
+
+/* beta_linspace (src/mpi_utils.cc:6-22), linear in beta, same FP64 steps. */
+int pticm_beta_linspace(double* beta, double T0, double T1, uint64_t nt, int inverse);
+
+/* initialize_replicas (src/initialization.cc:63-76): Bernoulli(1/2) spins
+ * from a counter-based stream, then a from-scratch field/energy pass. */
+int pticm_init_states(pticm_ctx* c, uint64_t seed);
+/* Explicit initial spins: R*n bytes (0/1), replica r = chain*nt + k. */
+int pticm_set_states(pticm_ctx* c, const uint8_t* states);
+
+/* The PT loop (src/solver.cc:67-127): `pt_steps` steps of sweeps, exchange
+ * and ICM. `phase_mask` selects phases (1 sweep, 2 exchange, 4 ICM; 7 = all)
+ * so that each phase can be checked on its own. */
+int pticm_run(pticm_ctx* c, uint64_t pt_steps, uint32_t phase_mask);
+
+typedef struct pticm_stats {
+    uint64_t pt_steps;      /* steps run so far                               */
+    uint64_t attempts;      /* spin-flip attempts (every visited site)        */
+    uint64_t flips;         /* accepted flips (num_of_flips, untruncated)     */
+    uint64_t swaps;         /* accepted exchanges (num_of_swaps)              */
+    uint32_t nt, chains, nc, replicas;
+    double last_run_ms;     /* device time of the last pticm_run (CUDA events)*/
+} pticm_stats;
+
+/* swap_attempts / swap_successes per slot (2*nt entries for two chains, as
+ * printed by src/solver.cc:152-153); either array may be NULL. */
+int pticm_get_stats(pticm_ctx* c, pticm_stats* s, uint64_t* swap_attempts, uint64_t* swap_successes);
+
+/* gather_best_energy_values (src/mpi_utils.cc:103-163): lowest energy seen
+ * by any replica, the replica's sweep counter then, and that state (n bytes). */
+int pticm_get_best(pticm_ctx* c, double* energy, uint64_t* sweep, uint8_t* state, int64_t* replica);
+
+/* Current replicas: states (R*n bytes), energies (R), local fields
+ * f_i = sum_j J_ij s_j (R*n, original site order) and the temperature slot
+ * of each replica.  Any pointer may be NULL. */
+int pticm_get_replicas(pticm_ctx* c, uint8_t* states, int64_t* energy, int32_t* fields, uint32_t* slot_of_replica);
+
+/* Ladder and slot -> replica map (beta_indices of src/replica_exchange.cc). */
+int pticm_get_ladder(pticm_ctx* c, double* beta, uint32_t* slot_to_replica, uint32_t* nc);
+
+/* From-scratch recompute of every replica's fields and energy on the GPU,
+ * compared with the incrementally tracked values; `mismatches` counts
+ * differing sites and energies (0 = bit-exact). */
+int pticm_verify(pticm_ctx* c, uint64_t* mismatches);
+
+/* --------------------------------------------------------------- replay -- */
+/* The reference's sequential algorithm driven by a recorded trace of its
+ * random decisions: per PT step, per sweep, per replica the uniforms
+ * Replica::sweep consumed (src/replica.cc:31-38), the exchange pair slots
+ * and log-uniforms (src/replica_exchange.cc:11-28), and the ICM seed sites
+ * (src/icm.cc:33).  The context must have chains == 2 and a ladder of
+ * distinct temperatures; its states are set with pticm_set_states. */
+typedef struct pticm_trace {
+    uint64_t pt_steps;
+    const double* uniforms;        /* all sweep uniforms, concatenated          */
+    uint64_t n_uniforms;
+    const uint64_t* sweep_offsets; /* pt_steps*sweeps*R + 1 offsets             */
+    const int32_t* xchg_slot;      /* pt_steps*2*(nt-1) slots                   */
+    const double* xchg_logu;
+    const int64_t* icm_seed;       /* pt_steps*nc seeds, original index or -1   */
+} pticm_trace;
+
+int pticm_replay(pticm_ctx* c, const pticm_trace* t);
+
+/* ----------------------------------------------------------- utilities -- */
+const char* pticm_last_error(void);
+const char* pticm_version(void);
+/* Philox4x32-10 known-answer probe: out[4*i..] = philox(ctr[4*i..], key[2*i..]). */
+int pticm_philox_probe(const uint32_t* ctr, const uint32_t* key, uint32_t* out, int count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

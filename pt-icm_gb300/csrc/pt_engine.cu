@@ -1,0 +1,960 @@
+// pt_engine.cu -- the PT-ICM engine for sm_103a.
+//
+// One persistent kernel runs `nsteps` parallel-tempering steps for a batch of
+// instances.  A step is, as in the reference's solve loop
+// (src/solver.cc:67-127):
+//   1. Metropolis sweeps of every replica        (src/replica.cc:5-38)
+//   2. replica exchange, chains*(nt-1) attempts  (src/replica_exchange.cc:5-100)
+//   3. isoenergetic cluster moves on the nc coldest temperatures
+//                                                (src/icm.cc:8-215)
+//
+// Layout: every replica of an instance lives in shared memory of the block
+// that owns it (int8 spins, int32 local fields f_i = sum_j J_ij s_j), the
+// adjacency is staged into shared memory by bulk (TMA) copies, and exchange
+// permutes the slot->replica map instead of moving spins.  A block owns `rpc`
+// replicas of one instance; `group` blocks share an instance and meet at a
+// bounded grid barrier once per step (cooperative launch).
+//
+// Production sweeps visit the sites colour class by colour class (no two
+// sites of a class are adjacent) with Philox uniforms compared against
+// per-temperature integer thresholds ceil(exp(-beta*dE) * 2^32), computed on
+// the host in FP64.  The replay variant visits sites in the reference's
+// sequential order and consumes a recorded uniform stream with FP64
+// exp(-beta*dE) tables, reproducing the reference bit for bit.
+#include <cstdint>
+#include <cstdio>
+
+#include "pticm_device.cuh"
+#include "pticm_engine.h"
+
+namespace pticm {
+
+template <typename T>
+__device__ __forceinline__ T* sm_ptr(uint8_t* base, uint32_t off) {
+    return reinterpret_cast<T*>(base + off);
+}
+
+// ------------------------------------------------------------ union-find
+// Concurrent union-find in shared memory: roots are hooked larger-under-
+// smaller with CAS (so parent pointers strictly decrease and no cycle can
+// form) and finds halve paths.  Retries are capped.
+__device__ __forceinline__ int uf_find(volatile int* parent, int x) {
+    for (int it = 0; it < (1 << 20); it++) {
+        const int p = parent[x];
+        if (p == x) return x;
+        const int gp = parent[p];
+        if (gp == p) return p;
+        parent[x] = gp;
+        x = gp;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ bool uf_unite(int* parent, int a, int b) {
+    volatile int* vp = parent;
+    for (int it = 0; it < (1 << 20); it++) {
+        a = uf_find(vp, a);
+        b = uf_find(vp, b);
+        if (a < 0 || b < 0) return false;
+        if (a == b) return true;
+        if (a < b) { const int t = a; a = b; b = t; }
+        if (atomicCAS(parent + a, a, b) == a) return true;
+    }
+    return false;
+}
+
+// ---------------------------------------------------------- team helpers
+// An ICM "team" is either one warp (many pairs per block) or the whole block
+// (one pair per block).  Sums go through a per-team shared scratch word.
+template <bool BLOCK>
+struct Team {
+    int tr, ts;                  // rank and size
+    long long* acc;              // team scratch (shared)
+    int* bcast;                  // team scratch (shared)
+    __device__ __forceinline__ void sync() const {
+        if (BLOCK) __syncthreads(); else __syncwarp();
+    }
+    __device__ __forceinline__ long long sum(long long v) const {
+        if (!BLOCK) {
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            return v;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) *acc = 0;
+        __syncthreads();
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(reinterpret_cast<unsigned long long*>(acc), (unsigned long long)v);
+        __syncthreads();
+        const long long r = *acc;
+        __syncthreads();
+        return r;
+    }
+};
+
+// Position of the r-th (0-based) set flag among d[0..n); one warp scans.
+__device__ __forceinline__ int select_rth(const uint8_t* d, int n, int r, int lane) {
+    int base = 0;
+    for (int c0 = 0; c0 < n; c0 += 32) {
+        const int i = c0 + lane;
+        const bool bit = (i < n) && d[i];
+        unsigned m = __ballot_sync(0xffffffffu, bit);
+        const int c = __popc(m);
+        if (r < base + c) {
+            for (int t = 0; t < r - base; t++) m &= m - 1;
+            return c0 + __ffs(m) - 1;
+        }
+        base += c;
+    }
+    return -1;
+}
+
+// Per-block view of the launch.
+struct BlockCtx {
+    InstanceDesc D;
+    int rank, r0;
+    const int32_t* row;
+    const uint32_t* adj;
+    int8_t* spin;
+    int32_t* field;
+    const int32_t* h;
+    long long* E;
+    uint32_t* slot;
+    uint32_t* rslot;
+    int32_t* tb;        // threshold row base of each local replica
+};
+
+// ------------------------------------------------------------------ ICM
+// One cluster move on the pair (A, B) = (slot a, slot b) at equal beta.  The
+// team computes the overlap, the reference's global-flip rule (src/icm.cc:
+// 20-28), a seed uniform among differing sites (src/icm.cc:33), the seed's
+// cluster of differing sites by union-find, and flips it in each member held
+// by this block.  Members held elsewhere are read from the published copy
+// and flipped by their own block, which computes the same cluster.
+template <bool BLOCK, bool REPLAY>
+__device__ void icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK>& team, int q,
+                         int rA, int rB, unsigned long long step, int ls, int* parent, uint8_t* d,
+                         int where_err) {
+    const InstanceDesc& D = B.D;
+    const int n = D.n, npad = D.n_pad;
+    const bool locA = rA >= B.r0 && rA < B.r0 + D.rpc;
+    const bool locB = rB >= B.r0 && rB < B.r0 + D.rpc;
+    const int parity = (int)(step & 1ull);
+    const int8_t* pubA = A.spins_pub + parity * A.spins_pub_half + D.spin_off + (long long)rA * npad;
+    const int8_t* pubB = A.spins_pub + parity * A.spins_pub_half + D.spin_off + (long long)rB * npad;
+    int8_t* sA = locA ? B.spin + (rA - B.r0) * npad : nullptr;
+    int8_t* sB = locB ? B.spin + (rB - B.r0) * npad : nullptr;
+    int32_t* fA = locA ? B.field + (rA - B.r0) * npad : nullptr;
+    int32_t* fB = locB ? B.field + (rB - B.r0) * npad : nullptr;
+
+    long long cl = 0;
+    for (int i = team.tr; i < n; i += team.ts) {
+        const int8_t a = locA ? sA[i] : ld_cg(pubA + i);
+        const int8_t b = locB ? sB[i] : ld_cg(pubB + i);
+        const uint8_t di = a != b;
+        d[i] = di;
+        cl += di;
+    }
+    team.sync();
+    long long cnt = team.sum(cl);
+    const bool gflip = cnt > (long long)(n / 2);
+    if (gflip) {
+        for (int i = team.tr; i < n; i += team.ts) {
+            if (locA) { sA[i] = (int8_t)-sA[i]; fA[i] = -fA[i]; }
+            d[i] ^= 1;
+        }
+        cnt = n - cnt;
+        team.sync();
+    }
+    bool moved = false;
+    if (REPLAY) {
+        const long long idx = (long long)ls * D.nc + q;
+        const long long traced = (idx < (long long)A.replay.n_icm) ? A.replay.icm_seed[idx] : -2;
+        if ((traced < 0) != (cnt == 0)) {
+            if (team.tr == 0) dev_fail(A.status, A.abort_flag, DEV_REPLAY_MISMATCH, where_err, idx, cnt);
+            return;
+        }
+        if (cnt > 0) {
+            if (traced >= n) {
+                if (team.tr == 0) dev_fail(A.status, A.abort_flag, DEV_BAD_INDEX, where_err + 1, idx, traced);
+                return;
+            }
+            const int seed = A.perm[D.perm_off + traced];
+            if (!d[seed]) {
+                if (team.tr == 0) dev_fail(A.status, A.abort_flag, DEV_REPLAY_MISMATCH, where_err + 2, idx, seed);
+                return;
+            }
+            if (team.tr == 0) *team.bcast = seed;
+        }
+    } else if (cnt > 0) {
+        const uint2 key = stream_key(A.seed, STREAM_ICM);
+        const uint4 rnd = philox4x32_10(make_uint4((uint32_t)q, (uint32_t)D.inst_id, (uint32_t)step,
+                                                   (uint32_t)(step >> 32)), key);
+        const int r = (int)bounded32(rnd.x, (uint32_t)cnt);
+        if (team.tr < 32) {
+            const int s = select_rth(d, n, r, team.tr);
+            if (team.tr == 0) *team.bcast = s;
+        }
+    }
+    team.sync();
+    if (cnt > 0) {
+        const int seed = *team.bcast;
+        if (seed < 0 || seed >= n) {
+            if (team.tr == 0) dev_fail(A.status, A.abort_flag, DEV_BAD_INDEX, where_err + 4, q, seed);
+            return;
+        }
+        for (int i = team.tr; i < n; i += team.ts) parent[i] = i;
+        team.sync();
+        bool ok = true;
+        for (int u = team.tr; u < n; u += team.ts) {
+            if (!d[u]) continue;
+            const int e0 = B.row[u], e1 = B.row[u + 1];
+            for (int a = e0; a < e1; a++) {
+                const int v = (int)(B.adj[a] >> 8);
+                if (v > u && d[v]) ok &= uf_unite(parent, u, v);
+            }
+        }
+        if (!ok) dev_fail(A.status, A.abort_flag, DEV_UF_LIMIT, where_err + 3, q, 0);
+        team.sync();
+        const int root = uf_find(parent, seed);
+        for (int i = team.tr; i < n; i += team.ts) {
+            if (!d[i]) continue;
+            if (uf_find(parent, i) != root) continue;
+            const int e0 = B.row[i], e1 = B.row[i + 1];
+            if (locA) {
+                const int s = sA[i];
+                sA[i] = (int8_t)-s;
+                for (int a = e0; a < e1; a++) {
+                    const uint32_t e = B.adj[a];
+                    atomicAdd(fA + (e >> 8), (int)(int8_t)(e & 0xffu) * (-2 * s));
+                }
+            }
+            if (locB) {
+                const int s = sB[i];
+                sB[i] = (int8_t)-s;
+                for (int a = e0; a < e1; a++) {
+                    const uint32_t e = B.adj[a];
+                    atomicAdd(fB + (e >> 8), (int)(int8_t)(e & 0xffu) * (-2 * s));
+                }
+            }
+        }
+        moved = true;
+        team.sync();
+    }
+    // energies of the members held here: E = sum h s + 1/2 sum s f
+    if (locA && (moved || gflip)) {
+        long long v = 0;
+        for (int i = team.tr; i < n; i += team.ts) v += (long long)sA[i] * (2 * (D.has_h ? B.h[i] : 0) + fA[i]);
+        v = team.sum(v);
+        if (team.tr == 0) B.E[rA] = v / 2;
+    }
+    if (locB && moved) {
+        long long v = 0;
+        for (int i = team.tr; i < n; i += team.ts) v += (long long)sB[i] * (2 * (D.has_h ? B.h[i] : 0) + fB[i]);
+        v = team.sum(v);
+        if (team.tr == 0) B.E[rB] = v / 2;
+    }
+    team.sync();
+}
+
+
+// --------------------------------------------------------------- sweeps
+// Colour-class Metropolis sweep of the block's replicas (production).
+// dE_i = -2 s_i (h_i + f_i); accepted with probability min(1, exp(-beta dE))
+// (src/replica.cc:31-38); an accepted flip pushes J_ij * (-2 s_i) into each
+// neighbour's field (the integer form of src/problem.cc:164-181).
+__device__ void colored_sweep(const EngineArgs& A, const BlockCtx& B, unsigned long long sweep_idx,
+                              int32_t* s_col, const uint32_t* s_thr, int* s_dEp, unsigned* s_flp,
+                              unsigned long long* s_flips, long long* s_bestE, int* s_improved,
+                              int* s_misc, bool best_per_phase) {
+    const InstanceDesc& D = B.D;
+    const int T = blockDim.x, tid = threadIdx.x;
+    const int npad = D.n_pad, rpc = D.rpc;
+    ThreadRng rng;
+    rng.start(stream_key(A.seed, STREAM_SWEEP), blockIdx.x * blockDim.x + tid, sweep_idx);
+    for (int c = 0; c < D.ncolors; c++) {
+        const int c0 = s_col[c];
+        const int Sc = s_col[c + 1] - c0;
+        const int items = rpc * Sc;
+        for (int it = tid; it < items; it += T) {
+            const int j = it / Sc;
+            const int i = c0 + (it - j * Sc);
+            int8_t* sp = B.spin + j * npad;
+            int32_t* fd = B.field + j * npad;
+            const int s = sp[i];
+            const int f = fd[i] + (D.has_h ? B.h[i] : 0);
+            const int de = -2 * s * f;
+            bool acc = de <= 0;
+            if (!acc) {
+                const uint32_t thr = s_thr[B.tb[j] + min(de >> 1, D.kmax)];
+                acc = (rng.next() < thr) || (thr == 0xFFFFFFFFu);
+            }
+            if (acc) {
+                sp[i] = (int8_t)-s;
+                atomicAdd(s_dEp + j, de);
+                atomicAdd(s_flp + j, 1u);
+                const int dl = -2 * s;
+                const int e0 = B.row[i], e1 = B.row[i + 1];
+                for (int a = e0; a < e1; a++) {
+                    const uint32_t e = B.adj[a];
+                    atomicAdd(fd + (e >> 8), (int)(int8_t)(e & 0xffu) * dl);
+                }
+            }
+        }
+        __syncthreads();
+        if (!best_per_phase && c + 1 < D.ncolors) continue;
+        // phase boundary: fold the phase's energy change, track the best state
+        for (int jj = tid; jj < rpc; jj += T) {
+            const int r = B.r0 + jj;
+            const long long E = B.E[r] + s_dEp[jj];
+            B.E[r] = E;
+            s_dEp[jj] = 0;
+            s_flips[jj] += s_flp[jj];
+            s_flp[jj] = 0;
+            const bool imp = E < s_bestE[jj];
+            s_improved[jj] = imp;
+            if (imp) {
+                s_bestE[jj] = E;
+                A.best_sweep[D.rep_off + r] = sweep_idx;
+                atomicAdd(s_misc + 1, 1);
+            }
+        }
+        __syncthreads();
+        if (s_misc[1] > 0) {
+            for (int idx = tid; idx < rpc * npad; idx += T) {
+                const int j = idx / npad;
+                if (s_improved[j]) A.best_state[D.spin_off + (long long)B.r0 * npad + idx] = B.spin[idx];
+            }
+            __syncthreads();
+            if (tid == 0) s_misc[1] = 0;
+            __syncthreads();
+        }
+    }
+}
+
+// Sequential sweep in the reference's site order (replay).  One warp per
+// replica: lane 0 makes each decision exactly as src/replica.cc:31-38 does
+// (dE <= 0, else u < exp(-beta*dE) with a recorded u), the warp applies the
+// field update and copies a new best state (src/replica.cc:18-29).
+__device__ void replay_sweep(const EngineArgs& A, const BlockCtx& B, int ls, int sw,
+                             unsigned long long sweep_idx, const double* s_ptab,
+                             unsigned long long* s_flips, long long* s_bestE) {
+    const InstanceDesc& D = B.D;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int n = D.n, npad = D.n_pad, kst = D.kmax + 1;
+    for (int j = warp; j < D.rpc; j += nw) {
+        const int r = B.r0 + j;
+        int8_t* sp = B.spin + j * npad;
+        int32_t* fd = B.field + j * npad;
+        const long long oi = ((long long)ls * A.sweeps + sw) * D.R + r;
+        unsigned long long pos = A.replay.sweep_offsets[oi];
+        const unsigned long long end = A.replay.sweep_offsets[oi + 1];
+        const int pbase = (int)(B.rslot[j] % (uint32_t)D.nt) * kst;
+        long long E = B.E[r];
+        long long bestE = s_bestE[j];
+        unsigned long long flips = 0;
+        bool bad = false;
+        for (int o = 0; o < n; o++) {
+            const int i = A.perm[D.perm_off + o];
+            int acc = 0, s = 0, de = 0;
+            if (lane == 0) {
+                s = sp[i];
+                const int f = fd[i] + (D.has_h ? B.h[i] : 0);
+                de = -2 * s * f;
+                if (de <= 0) {
+                    acc = 1;
+                } else {
+                    double u = 1.0;
+                    if (pos < end && pos < A.replay.n_uniforms) u = A.replay.uniforms[pos];
+                    else bad = true;
+                    pos++;
+                    acc = u < s_ptab[pbase + min(de >> 1, D.kmax)];
+                }
+            }
+            acc = __shfl_sync(0xffffffffu, acc, 0);
+            if (!acc) continue;
+            s = __shfl_sync(0xffffffffu, s, 0);
+            de = __shfl_sync(0xffffffffu, de, 0);
+            if (lane == 0) sp[i] = (int8_t)-s;
+            const int e0 = B.row[i], e1 = B.row[i + 1];
+            for (int a = e0 + lane; a < e1; a += 32) {
+                const uint32_t e = B.adj[a];
+                atomicAdd(fd + (e >> 8), (int)(int8_t)(e & 0xffu) * (-2 * s));
+            }
+            E += de;
+            flips++;
+            __syncwarp();
+            if (E < bestE) {
+                bestE = E;
+                for (int x = lane; x < npad; x += 32) A.best_state[D.spin_off + (long long)r * npad + x] = sp[x];
+                if (lane == 0) A.best_sweep[D.rep_off + r] = sweep_idx;
+            }
+            __syncwarp();
+        }
+        if (lane == 0) {
+            if (bad || pos != end) dev_fail(A.status, A.abort_flag, DEV_REPLAY_MISMATCH, 10, oi, (long long)(end - pos));
+            B.E[r] = E;
+            s_bestE[j] = bestE;
+            s_flips[j] += flips;
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------------- exchange
+// Production exchange with the reference's attempt order
+// (src/replica_exchange.cc:5-100): a shuffled order of the nt-1 adjacent
+// pairs is walked by one cursor shared by all chains (attempt a goes to chain
+// a % chains); the order is reshuffled whenever the cursor wraps.  Attempt
+// on pair k accepts iff dBeta*dE > 0 or log u < dBeta*dE, and swaps the
+// slot->replica entries.  Within one pass over the order each pair appears
+// once, so an attempt depends only on earlier attempts on the neighbouring
+// pairs of its chain: attempts are grouped into dependency levels and each
+// level runs in parallel, with exactly the sequential semantics.
+__device__ void exchange_reference_order(const EngineArgs& A, const BlockCtx& B, unsigned long long step,
+                                         uint32_t* s_order, const double* s_dbeta, unsigned* s_att,
+                                         unsigned* s_succ, float* s_xlogu, uint32_t* s_xrand,
+                                         int* s_lvl, uint32_t* s_tmp, int* s_misc) {
+    const InstanceDesc& D = B.D;
+    const int tid = threadIdx.x, T = blockDim.x;
+    const int nt = D.nt, C = D.chains, m = nt - 1;
+    if (m <= 0) return;
+    const int total = C * m;
+    // pre-draw: total log-uniforms and total shuffle keys
+    const uint2 key = stream_key(A.seed, STREAM_EXCHANGE);
+    const int ndraw = 2 * total;
+    for (int call = tid; call * 4 < ndraw; call += T) {
+        const uint4 r = philox4x32_10(make_uint4((uint32_t)call, (uint32_t)D.inst_id, (uint32_t)step,
+                                                 (uint32_t)(step >> 32)), key);
+        const uint32_t v[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int dix = call * 4 + q;
+            if (dix < total) s_xlogu[dix] = __logf(u01_open0(v[q]));
+            else if (dix < ndraw) s_xrand[dix - total] = v[q];
+        }
+    }
+    __syncthreads();
+    for (int round = 0; round < C; round++) {
+        // level of attempt i = 1 + max level of earlier attempts on pairs
+        // order[i]-1 and order[i]+1 of the same chain
+        for (int i = tid; i < m; i += T) {
+            s_lvl[i] = 1;
+            s_tmp[s_order[i]] = (uint32_t)i;   // position of each pair in this pass
+        }
+        __syncthreads();
+        for (;;) {
+            int changed = 0;
+            for (int i = tid; i < m; i += T) {
+                const int kb = (int)s_order[i];
+                const int c = (round * m + i) % C;
+                int lv = 1;
+                if (kb > 0) {
+                    const int jn = (int)s_tmp[kb - 1];
+                    if (jn < i && (round * m + jn) % C == c) lv = max(lv, ((volatile int*)s_lvl)[jn] + 1);
+                }
+                if (kb + 1 < m) {
+                    const int jn = (int)s_tmp[kb + 1];
+                    if (jn < i && (round * m + jn) % C == c) lv = max(lv, ((volatile int*)s_lvl)[jn] + 1);
+                }
+                if (lv != s_lvl[i]) { s_lvl[i] = lv; changed = 1; }
+            }
+            if (!__syncthreads_or(changed)) break;
+        }
+        int maxl = 0;
+        for (int i = tid; i < m; i += T) maxl = max(maxl, s_lvl[i]);
+        if (tid == 0) s_misc[2] = 0;
+        __syncthreads();
+        if (maxl) atomicMax(s_misc + 2, maxl);
+        __syncthreads();
+        const int L = s_misc[2];
+        for (int lv = 1; lv <= L; lv++) {
+            for (int i = tid; i < m; i += T) {
+                if (s_lvl[i] != lv) continue;
+                const int kb = (int)s_order[i];
+                const int a = round * m + i;
+                const int c = a % C;
+                const int k = c * nt + kb;
+                const uint32_t r1 = B.slot[k], r2 = B.slot[k + 1];
+                const double x = s_dbeta[kb] * (double)(B.E[r1] - B.E[r2]);
+                s_att[k]++;
+                if (x > 0.0 || (double)s_xlogu[a] < x) {
+                    s_succ[k]++;
+                    B.slot[k] = r2;
+                    B.slot[k + 1] = r1;
+                }
+            }
+            __syncthreads();
+        }
+        // reshuffle: rank the pairs by fresh random keys (ties by position)
+        const uint32_t* keys = s_xrand + round * m;
+        for (int i = tid; i < m; i += T) {
+            const uint32_t ki = keys[i];
+            int rank = 0;
+            for (int j = 0; j < m; j++) {
+                const uint32_t kj = keys[j];
+                rank += (kj < ki) || (kj == ki && j < i);
+            }
+            s_tmp[rank] = s_order[i];
+        }
+        __syncthreads();
+        for (int i = tid; i < m; i += T) s_order[i] = s_tmp[i];
+        __syncthreads();
+    }
+}
+
+// Deterministic even/odd exchange: per chain, all even pairs, then all odd
+// pairs, each set in parallel (nt-1 attempts per chain per step).
+__device__ void exchange_even_odd(const EngineArgs& A, const BlockCtx& B, unsigned long long step,
+                                  const double* s_dbeta, unsigned* s_att, unsigned* s_succ) {
+    const InstanceDesc& D = B.D;
+    const int tid = threadIdx.x, T = blockDim.x;
+    const int nt = D.nt, C = D.chains, m = nt - 1;
+    const uint2 key = stream_key(A.seed, STREAM_EXCHANGE);
+    for (int par = 0; par < 2; par++) {
+        const int per_chain = (m - par + 1) / 2;   // pairs kb = par, par+2, ...
+        const int total = C * per_chain;
+        for (int t = tid; t < total; t += T) {
+            const int c = t / per_chain;
+            const int kb = par + 2 * (t - c * per_chain);
+            const int k = c * nt + kb;
+            const uint4 r = philox4x32_10(make_uint4((uint32_t)(k | (par << 30)), (uint32_t)D.inst_id,
+                                                     (uint32_t)step, (uint32_t)(step >> 32)), key);
+            const uint32_t r1 = B.slot[k], r2 = B.slot[k + 1];
+            const double x = s_dbeta[kb] * (double)(B.E[r1] - B.E[r2]);
+            s_att[k]++;
+            if (x > 0.0 || (double)__logf(u01_open0(r.x)) < x) {
+                s_succ[k]++;
+                B.slot[k] = r2;
+                B.slot[k + 1] = r1;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Replayed exchange: the recorded pair sequence and log-uniforms, applied
+// sequentially in FP64 exactly as src/replica_exchange.cc:20-40 computes.
+__device__ void exchange_replay(const EngineArgs& A, const BlockCtx& B, int ls, const double* s_beta,
+                                unsigned* s_att, unsigned* s_succ) {
+    const InstanceDesc& D = B.D;
+    if (threadIdx.x == 0) {
+        const int nt = D.nt, per = D.chains * (nt - 1);
+        for (int t = 0; t < per; t++) {
+            const long long idx = (long long)ls * per + t;
+            if (idx >= (long long)A.replay.n_xchg) {
+                dev_fail(A.status, A.abort_flag, DEV_REPLAY_MISMATCH, 20, idx, 0);
+                break;
+            }
+            const int k = A.replay.xchg_slot[idx];
+            if (k < 0 || k + 1 >= D.R || (k % nt) == nt - 1) {
+                dev_fail(A.status, A.abort_flag, DEV_BAD_INDEX, 21, idx, k);
+                break;
+            }
+            const int kb = k % nt;
+            const uint32_t r1 = B.slot[k], r2 = B.slot[k + 1];
+            const double dB = __dsub_rn(s_beta[kb], s_beta[kb + 1]);
+            const double dE = (double)(B.E[r1] - B.E[r2]);
+            const double x = __dmul_rn(dB, dE);
+            s_att[k]++;
+            if (__dmul_rn(dE, dB) > 0.0 || A.replay.xchg_logu[idx] < x) {
+                s_succ[k]++;
+                B.slot[k] = r2;
+                B.slot[k + 1] = r1;
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------- kernel
+template <bool REPLAY, bool BLOCKTEAM>
+__global__ void __launch_bounds__(1024) pt_engine_kernel(const EngineArgs A) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    const SmemPlan& S = A.sm;
+    const int tid = threadIdx.x, T = blockDim.x;
+    BlockCtx B;
+    const int inst = A.block_inst[blockIdx.x];
+    B.D = A.desc[inst];
+    const InstanceDesc& D = B.D;
+    B.rank = blockIdx.x - D.first_block;
+    B.r0 = B.rank * D.rpc;
+    const int n = D.n, npad = D.n_pad, R = D.R, nt = D.nt, rpc = D.rpc, kst = D.kmax + 1;
+    volatile int* abortf = A.abort_flag;
+
+    uint64_t* mbar = sm_ptr<uint64_t>(smem, S.mbar);
+    int32_t* s_col = sm_ptr<int32_t>(smem, S.col);
+    int32_t* s_h = sm_ptr<int32_t>(smem, S.h);
+    B.spin = sm_ptr<int8_t>(smem, S.spin);
+    B.field = sm_ptr<int32_t>(smem, S.field);
+    uint32_t* s_thr = sm_ptr<uint32_t>(smem, S.thr);
+    double* s_ptab = sm_ptr<double>(smem, S.ptab);
+    B.slot = sm_ptr<uint32_t>(smem, S.slot);
+    B.rslot = sm_ptr<uint32_t>(smem, S.rslot);
+    B.tb = sm_ptr<int32_t>(smem, S.rslot) + rpc;
+    uint32_t* s_order = sm_ptr<uint32_t>(smem, S.order);
+    double* s_beta = sm_ptr<double>(smem, S.beta);
+    double* s_dbeta = sm_ptr<double>(smem, S.dbeta);
+    B.E = sm_ptr<long long>(smem, S.E);
+    int* s_dEp = sm_ptr<int>(smem, S.dEp);
+    unsigned* s_flp = sm_ptr<unsigned>(smem, S.flp);
+    long long* s_bestE = sm_ptr<long long>(smem, S.bestE);
+    unsigned long long* s_flips = sm_ptr<unsigned long long>(smem, S.flips);
+    int* s_improved = sm_ptr<int>(smem, S.improved);
+    unsigned* s_att = sm_ptr<unsigned>(smem, S.att);
+    unsigned* s_succ = sm_ptr<unsigned>(smem, S.succ);
+    float* s_xlogu = sm_ptr<float>(smem, S.xlogu);
+    uint32_t* s_xrand = sm_ptr<uint32_t>(smem, S.xrand);
+    int* s_lvl = sm_ptr<int>(smem, S.xlevel);
+    uint32_t* s_tmp = sm_ptr<uint32_t>(smem, S.xpos);
+    uint8_t* s_icm = smem + S.icm;
+    int* s_misc = sm_ptr<int>(smem, S.misc);
+    long long* s_team_acc = sm_ptr<long long>(smem, S.misc + 64);
+    int* s_team_bc = sm_ptr<int>(smem, S.misc + 64 + 8 * 32);
+
+    const int32_t* g_row = A.row + D.row_off;
+    const uint32_t* g_adj = A.adj + D.adj_off;
+    B.h = D.has_h ? s_h : nullptr;
+
+    // ---- stage the adjacency (bulk copies) and load the block's state
+    if (S.stage_adj) {
+        int32_t* s_row = sm_ptr<int32_t>(smem, S.row);
+        uint32_t* s_adj = sm_ptr<uint32_t>(smem, S.adj);
+        if (tid == 0) mbar_init(mbar, 1);
+        __syncthreads();
+        if (tid == 0) {
+            const uint32_t rb = (uint32_t)(((n + 1) * 4 + 15) & ~15);
+            const uint32_t ab = (uint32_t)((D.nnz * 4 + 15) & ~15);
+            mbar_expect_tx(mbar, rb + ab);
+            bulk_g2s(s_row, g_row, rb, mbar);
+            if (ab) bulk_g2s(s_adj, g_adj, ab, mbar);
+        }
+        B.row = s_row;
+        B.adj = s_adj;
+    } else {
+        B.row = g_row;
+        B.adj = g_adj;
+    }
+    for (int i = tid; i <= D.ncolors; i += T) s_col[i] = A.col[D.col_off + i];
+    if (D.has_h)
+        for (int i = tid; i < n; i += T) s_h[i] = A.hpool[D.h_off + i];
+    {
+        const long long base = D.spin_off + (long long)B.r0 * npad;
+        for (int idx = tid; idx < rpc * npad; idx += T) {
+            B.spin[idx] = A.spins[base + idx];
+            B.field[idx] = A.fields[base + idx];
+        }
+    }
+    for (int r = tid; r < R; r += T) {
+        B.slot[r] = A.slot_rep[D.rep_off + r];
+        B.E[r] = A.energy[D.rep_off + r];
+        s_att[r] = 0;
+        s_succ[r] = 0;
+    }
+    for (int k = tid; k < nt; k += T) {
+        s_order[k] = A.xorder[D.rep_off + k];
+        s_beta[k] = A.beta[D.beta_off + k];
+    }
+    for (int k = tid; k < nt * kst; k += T) {
+        s_thr[k] = A.thr[D.thr_off + k];
+        if (REPLAY) s_ptab[k] = A.ptab[D.ptab_off + k];
+    }
+    for (int j = tid; j < rpc; j += T) {
+        s_bestE[j] = A.best_E[D.rep_off + B.r0 + j];
+        s_flips[j] = 0;
+        s_dEp[j] = 0;
+        s_flp[j] = 0;
+        s_improved[j] = 0;
+    }
+    if (tid < 8) s_misc[tid] = 0;
+    __syncthreads();
+    for (int k = tid; k + 1 < nt; k += T) s_dbeta[k] = s_beta[k] - s_beta[k + 1];
+    for (int s = tid; s < R; s += T) {
+        const uint32_t r = B.slot[s];
+        if ((int)r >= B.r0 && (int)r < B.r0 + rpc) {
+            B.rslot[r - B.r0] = (uint32_t)s;
+            B.tb[r - B.r0] = (int)(((uint32_t)s % (uint32_t)nt) * (uint32_t)kst);
+        }
+    }
+    if (S.stage_adj) {
+        if (!mbar_wait_bounded(mbar, 0) && tid == 0) dev_fail(A.status, A.abort_flag, DEV_TMA_TIMEOUT, 2, blockIdx.x, 0);
+    }
+    __syncthreads();
+
+    const bool icm_on = (A.phase_mask & PHASE_ICM) && D.nc > 0 && D.chains >= 2;
+    const bool best_pp = (A.flags & ENGINE_BEST_PER_PHASE) != 0;
+    for (int ls = 0; ls < A.nsteps; ls++) {
+        if (tid == 0) s_misc[3] = *abortf;
+        __syncthreads();
+        if (s_misc[3]) break;
+        const unsigned long long step = A.step0 + (unsigned long long)ls;
+        const int parity = (int)(step & 1ull);
+        if (A.phase_mask & PHASE_SWEEP) {
+            for (int sw = 0; sw < A.sweeps; sw++) {
+                const unsigned long long sweep_idx = step * (unsigned long long)A.sweeps + (unsigned long long)sw;
+                if (REPLAY) {
+                    replay_sweep(A, B, ls, sw, sweep_idx, s_ptab, s_flips, s_bestE);
+                    __syncthreads();
+                } else {
+                    colored_sweep(A, B, sweep_idx, s_col, s_thr, s_dEp, s_flp, s_flips, s_bestE, s_improved,
+                                  s_misc, best_pp);
+                }
+            }
+        }
+        if (D.group > 1) {
+            // publish this block's energies (and spins, for ICM partners)
+            for (int j = tid; j < rpc; j += T) A.energy_pub[parity * A.energy_pub_half + D.rep_off + B.r0 + j] = B.E[B.r0 + j];
+            if (icm_on) {
+                const long long base = parity * A.spins_pub_half + D.spin_off + (long long)B.r0 * npad;
+                for (int idx = tid; idx < rpc * npad; idx += T) A.spins_pub[base + idx] = B.spin[idx];
+            }
+            if (!group_barrier(A.bar + 2 * inst, (unsigned)D.group, abortf, A.status)) break;
+            for (int r = tid; r < R; r += T)
+                if (r < B.r0 || r >= B.r0 + rpc) B.E[r] = ld_cg(A.energy_pub + parity * A.energy_pub_half + D.rep_off + r);
+            __syncthreads();
+        }
+        if (A.phase_mask & PHASE_EXCHANGE) {
+            if (REPLAY) exchange_replay(A, B, ls, s_beta, s_att, s_succ);
+            else if (A.flags & ENGINE_EXCHANGE_EVEN_ODD) exchange_even_odd(A, B, step, s_dbeta, s_att, s_succ);
+            else exchange_reference_order(A, B, step, s_order, s_dbeta, s_att, s_succ, s_xlogu, s_xrand, s_lvl, s_tmp, s_misc);
+            for (int s = tid; s < R; s += T) {
+                const uint32_t r = B.slot[s];
+                if ((int)r >= B.r0 && (int)r < B.r0 + rpc) {
+                    B.rslot[r - B.r0] = (uint32_t)s;
+                    B.tb[r - B.r0] = (int)(((uint32_t)s % (uint32_t)nt) * (uint32_t)kst);
+                }
+            }
+            __syncthreads();
+        }
+        if (icm_on) {
+            // pairs q = cp*nc + kk: slots (2cp)*nt + k and (2cp+1)*nt + k, k = nt-1-kk
+            const int npairs = D.nc * (D.chains / 2);
+            if (BLOCKTEAM) {
+                Team<true> team{tid, T, s_team_acc, s_team_bc};
+                int* parent = reinterpret_cast<int*>(s_icm);
+                uint8_t* d = s_icm + (size_t)S.max_n_pad * 4;
+                for (int q = 0; q < npairs; q++) {
+                    const int cp = q / D.nc, kk = q - cp * D.nc, k = nt - 1 - kk;
+                    const int rA = (int)B.slot[(2 * cp) * nt + k], rB = (int)B.slot[(2 * cp + 1) * nt + k];
+                    const bool mine = (rA >= B.r0 && rA < B.r0 + rpc) || (rB >= B.r0 && rB < B.r0 + rpc);
+                    if (!mine) continue;
+                    icm_pair<true, REPLAY>(A, B, team, q, rA, rB, step, ls, parent, d, 30);
+                }
+            } else {
+                const int warp = tid >> 5, lane = tid & 31;
+                const int teams = min(S.teams, T >> 5);
+                if (warp < teams) {
+                    Team<false> team{lane, 32, s_team_acc + warp, s_team_bc + warp};
+                    int* parent = reinterpret_cast<int*>(s_icm + (size_t)warp * S.icm_team_bytes);
+                    uint8_t* d = s_icm + (size_t)warp * S.icm_team_bytes + (size_t)S.max_n_pad * 4;
+                    int e = 0;
+                    for (int q = 0; q < npairs; q++) {
+                        const int cp = q / D.nc, kk = q - cp * D.nc, k = nt - 1 - kk;
+                        const int rA = (int)B.slot[(2 * cp) * nt + k], rB = (int)B.slot[(2 * cp + 1) * nt + k];
+                        const bool mine = (rA >= B.r0 && rA < B.r0 + rpc) || (rB >= B.r0 && rB < B.r0 + rpc);
+                        if (!mine) continue;
+                        if ((e++ % teams) != warp) continue;
+                        icm_pair<false, REPLAY>(A, B, team, q, rA, rB, step, ls, parent, d, 30);
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    __syncthreads();
+    // ---- write the block's state back
+    {
+        const long long base = D.spin_off + (long long)B.r0 * npad;
+        for (int idx = tid; idx < rpc * npad; idx += T) {
+            A.spins[base + idx] = B.spin[idx];
+            A.fields[base + idx] = B.field[idx];
+        }
+    }
+    for (int j = tid; j < rpc; j += T) {
+        const long long g = D.rep_off + B.r0 + j;
+        A.energy[g] = B.E[B.r0 + j];
+        A.best_E[g] = s_bestE[j];
+        A.flips[g] += s_flips[j];
+    }
+    if (B.rank == 0) {
+        for (int r = tid; r < R; r += T) {
+            A.slot_rep[D.rep_off + r] = B.slot[r];
+            A.attempts[D.rep_off + r] += s_att[r];
+            A.successes[D.rep_off + r] += s_succ[r];
+        }
+        for (int k = tid; k < nt; k += T) A.xorder[D.rep_off + k] = s_order[k];
+    }
+}
+
+// --------------------------------------------------- from-scratch checks
+// For every replica: fields f_i = sum_j J_ij s_j, E = sum h s + 1/2 sum s f
+// and the cut sum over edges of w [s_i != s_j] (src/problem.cc:33-162),
+// compared with the tracked fields and energy.  One block per replica.
+__global__ void recompute_kernel(const EngineArgs A, const int32_t* rep_inst, int total_reps, int write_back,
+                                 unsigned long long* mismatches, long long* E_out, long long* cut2_out) {
+    const int g = blockIdx.x;
+    if (g >= total_reps) return;
+    const InstanceDesc D = A.desc[rep_inst[g]];
+    const int r = (int)(g - D.rep_off);
+    const int8_t* s = A.spins + D.spin_off + (long long)r * D.n_pad;
+    int32_t* f = A.fields + D.spin_off + (long long)r * D.n_pad;
+    const int32_t* row = A.row + D.row_off;
+    const uint32_t* adj = A.adj + D.adj_off;
+    long long e2 = 0, cut2 = 0;
+    unsigned long long bad = 0;
+    for (int i = threadIdx.x; i < D.n; i += blockDim.x) {
+        int fi = 0;
+        long long ci = 0;
+        const int si = s[i];
+        for (int a = row[i]; a < row[i + 1]; a++) {
+            const uint32_t e = adj[a];
+            const int J = (int)(int8_t)(e & 0xffu);
+            const int sv = s[e >> 8];
+            fi += J * sv;
+            if (sv != si) ci += J;
+        }
+        const int hi = D.has_h ? A.hpool[D.h_off + i] : 0;
+        e2 += (long long)si * (2 * hi + fi);
+        cut2 += ci;
+        if (si != 1 && si != -1) bad++;
+        if (write_back) f[i] = fi;
+        else if (f[i] != fi) bad++;
+    }
+    __shared__ long long red[3][32];
+    for (int o = 16; o > 0; o >>= 1) {
+        e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+        cut2 += __shfl_xor_sync(0xffffffffu, cut2, o);
+        bad += __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if (l == 0) { red[0][w] = e2; red[1][w] = cut2; red[2][w] = (long long)bad; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long te = 0, tc = 0, tb = 0;
+        for (int k = 0; k < nw; k++) { te += red[0][k]; tc += red[1][k]; tb += red[2][k]; }
+        const long long E = te / 2;
+        if (write_back) A.energy[g] = E;
+        else if (A.energy[g] != E) tb++;
+        if (E_out) E_out[g] = E;
+        if (cut2_out) cut2_out[g] = tc;
+        if (mismatches) atomicAdd(mismatches, (unsigned long long)tb);
+    }
+}
+
+// Bernoulli(1/2) initial spins from the Philox init stream.
+__global__ void init_spins_kernel(const EngineArgs A, const int32_t* rep_inst, int total_reps,
+                                  unsigned long long seed) {
+    const int g = blockIdx.x;
+    if (g >= total_reps) return;
+    const InstanceDesc D = A.desc[rep_inst[g]];
+    const int r = (int)(g - D.rep_off);
+    int8_t* s = A.spins + D.spin_off + (long long)r * D.n_pad;
+    const uint2 key = stream_key(seed, STREAM_INIT);
+    for (int i4 = threadIdx.x; i4 * 4 < D.n_pad; i4 += blockDim.x) {
+        const uint4 x = philox4x32_10(make_uint4((uint32_t)i4, (uint32_t)r, (uint32_t)D.inst_id, 0x5EEDu), key);
+        const uint32_t v[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int i = i4 * 4 + q;
+            if (i < D.n_pad) s[i] = (i < D.n) ? (int8_t)((v[q] >> 31) ? 1 : -1) : (int8_t)1;
+        }
+    }
+}
+
+// Philox outputs for host-side known-answer checks.
+__global__ void philox_probe_kernel(const uint4* ctr, const uint2* key, uint4* out, int count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) out[i] = philox4x32_10(ctr[i], key[i]);
+}
+
+// Problem::energy / maxcut / calculate_dE for a batch of states (device
+// order, +-1): E, twice the cut, and dE_i = -2 s_i (h_i + f_i).
+__global__ void evaluate_kernel(const int32_t* row, const uint32_t* adj, const int32_t* h, int n, int n_pad,
+                                const int8_t* states, int count, long long* E_out, long long* cut2_out,
+                                int32_t* dE_out) {
+    const int g = blockIdx.x;
+    if (g >= count) return;
+    const int8_t* s = states + (long long)g * n_pad;
+    long long e2 = 0, cut2 = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        int fi = 0;
+        long long ci = 0;
+        const int si = s[i];
+        for (int a = row[i]; a < row[i + 1]; a++) {
+            const uint32_t e = adj[a];
+            const int J = (int)(int8_t)(e & 0xffu);
+            const int sv = s[e >> 8];
+            fi += J * sv;
+            if (sv != si) ci += J;
+        }
+        const int hi = h ? h[i] : 0;
+        e2 += (long long)si * (2 * hi + fi);
+        cut2 += ci;
+        if (dE_out) dE_out[(long long)g * n_pad + i] = -2 * si * (hi + fi);
+    }
+    __shared__ long long red[2][32];
+    for (int o = 16; o > 0; o >>= 1) {
+        e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+        cut2 += __shfl_xor_sync(0xffffffffu, cut2, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    if (l == 0) { red[0][w] = e2; red[1][w] = cut2; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long te = 0, tc = 0;
+        for (int k = 0; k < nw; k++) { te += red[0][k]; tc += red[1][k]; }
+        E_out[g] = te / 2;
+        cut2_out[g] = tc;
+    }
+}
+
+// ------------------------------------------------------------ launchers
+cudaError_t launch_engine(const EngineArgs& A, int threads, bool replay, bool block_team, bool cooperative,
+                          cudaStream_t stream) {
+    void* fn;
+    if (replay) fn = (void*)pt_engine_kernel<true, false>;
+    else if (block_team) fn = (void*)pt_engine_kernel<false, true>;
+    else fn = (void*)pt_engine_kernel<false, false>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)A.sm.total);
+    if (e != cudaSuccess) return e;
+    void* args[] = {(void*)&A};
+    if (cooperative)
+        return cudaLaunchCooperativeKernel(fn, dim3(A.n_blocks), dim3(threads), args, A.sm.total, stream);
+    return cudaLaunchKernel(fn, dim3(A.n_blocks), dim3(threads), args, A.sm.total, stream);
+}
+
+cudaError_t engine_max_blocks_per_sm(bool replay, bool block_team, int threads, size_t smem, int* out) {
+    const void* fn;
+    if (replay) fn = (const void*)pt_engine_kernel<true, false>;
+    else if (block_team) fn = (const void*)pt_engine_kernel<false, true>;
+    else fn = (const void*)pt_engine_kernel<false, false>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, fn, threads, smem);
+}
+
+cudaError_t launch_recompute(const EngineArgs& A, const int32_t* rep_inst, int total_reps, int write_back,
+                             unsigned long long* mismatches, long long* E_out, long long* cut2_out,
+                             cudaStream_t stream) {
+    recompute_kernel<<<total_reps, 256, 0, stream>>>(A, rep_inst, total_reps, write_back, mismatches, E_out, cut2_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_init_spins(const EngineArgs& A, const int32_t* rep_inst, int total_reps,
+                              unsigned long long seed, cudaStream_t stream) {
+    init_spins_kernel<<<total_reps, 256, 0, stream>>>(A, rep_inst, total_reps, seed);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_evaluate(const int32_t* row, const uint32_t* adj, const int32_t* h, int n, int n_pad,
+                            const int8_t* states, int count, long long* E_out, long long* cut2_out,
+                            int32_t* dE_out, cudaStream_t stream) {
+    evaluate_kernel<<<count, 256, 0, stream>>>(row, adj, h, n, n_pad, states, count, E_out, cut2_out, dE_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_philox_probe(const uint4* ctr, const uint2* key, uint4* out, int count, cudaStream_t stream) {
+    philox_probe_kernel<<<(count + 127) / 128, 128, 0, stream>>>(ctr, key, out, count);
+    return cudaGetLastError();
+}
+
+}  // namespace pticm

@@ -1,0 +1,203 @@
+// pticm_device.cuh -- device-side building blocks shared by the PT-ICM kernels
+// (sm_103a): counter-based RNG, bounded waits, bulk-copy staging, error words.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "pticm_engine.h"
+
+namespace pticm {
+
+// ------------------------------------------------------------------ errors
+// Device-side failures are recorded in one DevStatus word block; the first
+// failure wins.  Kernels never trap: they record, raise `abort`, and return.
+enum DevErr : int {
+    DEV_OK = 0,
+    DEV_BARRIER_TIMEOUT = 1,   // a group barrier waited longer than its limit
+    DEV_TMA_TIMEOUT = 2,       // a bulk-copy mbarrier never completed
+    DEV_UF_LIMIT = 3,          // union-find retry cap exceeded
+    DEV_REPLAY_MISMATCH = 4,   // a replay trace disagrees with the device state
+    DEV_BAD_INDEX = 5,         // an index failed a bounds check
+    DEV_ABORTED = 6,           // another block aborted first
+};
+
+__device__ __forceinline__ void dev_fail(DevStatus* st, volatile int* abort_flag, int err, int where,
+                                         long long a0 = 0, long long a1 = 0) {
+    if (atomicCAS(&st->error, 0, err) == 0) {
+        st->where = where;
+        st->aux0 = a0;
+        st->aux1 = a1;
+    }
+    *abort_flag = 1;
+    __threadfence();
+}
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Waits on other blocks give up after this many nanoseconds.
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;
+
+// --------------------------------------------------------------------- RNG
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3", SC'11): ten rounds of two 32x32->64 multiplies with
+// Weyl-sequence key increments.
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+        k.x += 0x9E3779B9u;
+        k.y += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// Independent Philox streams are separated by key: the run seed XOR a
+// per-purpose constant.
+enum StreamTag : uint32_t {
+    STREAM_SWEEP = 0x00000000u,
+    STREAM_EXCHANGE = 0x45584348u,  // "EXCH"
+    STREAM_ICM = 0x49434D31u,       // "ICM1"
+    STREAM_INIT = 0x494E4954u,      // "INIT"
+};
+
+__device__ __forceinline__ uint2 stream_key(unsigned long long seed, uint32_t tag) {
+    return make_uint2((uint32_t)seed ^ tag, (uint32_t)(seed >> 32) ^ (tag * 0x9E3779B9u));
+}
+
+// A per-thread buffered Philox stream: four 32-bit words per block call.
+struct ThreadRng {
+    uint4 buf;
+    uint32_t avail;
+    uint32_t calls;
+    uint4 ctr;   // (thread id, step lo, step hi, call index)
+    uint2 key;
+
+    __device__ __forceinline__ void start(uint2 k, uint32_t tid, unsigned long long step) {
+        key = k;
+        ctr = make_uint4(tid, (uint32_t)step, (uint32_t)(step >> 32), 0u);
+        avail = 0;
+        calls = 0;
+    }
+    __device__ __forceinline__ uint32_t next() {
+        if (avail == 0) {
+            ctr.w = calls++;
+            buf = philox4x32_10(ctr, key);
+            avail = 4;
+        }
+        const uint32_t r = buf.x;
+        buf.x = buf.y;
+        buf.y = buf.z;
+        buf.z = buf.w;
+        avail--;
+        return r;
+    }
+};
+
+// Uniform in (0, 1] from the top 24 bits (never zero, so log() is finite).
+__device__ __forceinline__ float u01_open0(uint32_t x) {
+    return ((float)(x >> 8) + 1.0f) * (1.0f / 16777216.0f);
+}
+
+// Integer in [0, range) by the high word of a 32x32 product (range < 2^32).
+__device__ __forceinline__ uint32_t bounded32(uint32_t x, uint32_t range) {
+    return __umulhi(x, range);
+}
+
+// ---------------------------------------------------- cross-block memory
+__device__ __forceinline__ long long ld_cg(const long long* p) { return __ldcg(p); }
+__device__ __forceinline__ int8_t ld_cg(const int8_t* p) { return (int8_t)__ldcg((const signed char*)p); }
+
+// -------------------------------------------------------- group barrier
+// A sense-counting barrier over `nblocks` co-resident blocks (guaranteed by
+// a cooperative launch).  Block arrival is counted in bar[0]; the last
+// arriver bumps the generation in bar[1].  Waits are bounded: after
+// kWaitLimitNs, or when another block has raised `abort`, the barrier
+// records the failure and returns false.  Callers return when it fails.
+__device__ __forceinline__ bool group_barrier(unsigned int* bar, unsigned int nblocks,
+                                              volatile int* abort_flag, DevStatus* st) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int* gen = bar + 1;
+        const unsigned int g = *gen;
+        __threadfence();
+        const unsigned int arrived = atomicAdd(bar, 1u);
+        int ok = 1;
+        if (arrived == nblocks - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            const unsigned long long t0 = globaltimer_ns();
+            unsigned int spins = 0;
+            while (*gen == g) {
+                if (*abort_flag) { ok = 0; break; }
+                if ((++spins & 63u) == 0 && globaltimer_ns() - t0 > kWaitLimitNs) {
+                    dev_fail(st, abort_flag, DEV_BARRIER_TIMEOUT, 1, blockIdx.x, g);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// ------------------------------------------------- bulk-copy (TMA) staging
+// One-dimensional cp.async.bulk global->shared copies completing on an
+// mbarrier.  Addresses must be 16-byte aligned and sizes multiples of 16.
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// Bounded wait for phase `parity` of an mbarrier; false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    const unsigned long long t0 = globaltimer_ns();
+    unsigned int spins = 0;
+    while (!mbar_try_wait(bar, parity)) {
+        if ((++spins & 255u) == 0 && globaltimer_ns() - t0 > kWaitLimitNs) return false;
+    }
+    return true;
+}
+
+}  // namespace pticm

@@ -1,0 +1,132 @@
+// pticm_engine.h -- layout contract between the host runtime and the PT-ICM
+// engine kernel.  Plain structs, shared by host (.cc) and device (.cu) code.
+#pragma once
+#include <cstdint>
+
+namespace pticm {
+
+// First device-side failure of a launch (error 0 = none).
+struct DevStatus {
+    int error;
+    int where;
+    long long aux0;
+    long long aux1;
+};
+
+// One PT instance (a graph and its 2..C replica chains) inside a launch.
+// Sites are renumbered so that colour classes are contiguous: site i of the
+// device layout is original site perm[i].  Every pool offset is in elements.
+struct InstanceDesc {
+    int32_t n;          // spins
+    int32_t n_pad;      // row stride of per-replica arrays (multiple of 16)
+    int32_t nnz;        // directed adjacency entries (2M for sparse inputs)
+    int32_t ncolors;    // colour classes
+    int32_t kmax;       // largest dE/2 = max_i (|h_i| + sum_j |J_ij|)
+    int32_t nt;         // temperatures per chain
+    int32_t chains;     // replicas per temperature
+    int32_t R;          // replicas = nt * chains
+    int32_t nc;         // ICM temperatures (coldest nc slots of each chain pair)
+    int32_t has_h;      // linear terms present
+    int32_t group;      // blocks that share this instance
+    int32_t rpc;        // replicas per block (R = group * rpc)
+    int32_t first_block;
+    int32_t inst_id;    // stable id used in RNG counters
+    int32_t pad0, pad1;
+    int64_t row_off;    // int32 pool: n+1 row starts (relative to the instance)
+    int64_t adj_off;    // uint32 pool: nnz packed entries (col << 8 | (uint8)J)
+    int64_t col_off;    // int32 pool: ncolors+1 colour-class starts
+    int64_t h_off;      // int32 pool: n linear terms
+    int64_t beta_off;   // double pool: nt values
+    int64_t thr_off;    // uint32 pool: nt*(kmax+1) acceptance thresholds
+    int64_t ptab_off;   // double pool: nt*(kmax+1) exp(-beta*dE) (replay)
+    int64_t rep_off;    // first replica of the instance in the replica pools
+    int64_t spin_off;   // first byte of the instance in the spin pools
+    int64_t perm_off;   // int32 pool: original site -> device site (replay)
+};
+
+// Shared-memory plan of a launch (bytes), identical for every block.
+struct SmemPlan {
+    uint32_t total;
+    uint32_t mbar;
+    uint32_t row, adj;          // staged adjacency (when stage_adj)
+    uint32_t col, h;
+    uint32_t spin, field;       // rpc * n_pad
+    uint32_t thr;               // rpc * (kmax+1)
+    uint32_t ptab;              // replay: nt * (kmax+1) doubles
+    uint32_t slot, rslot, order, beta, dbeta;
+    uint32_t E, dEp, flp, bestE, flips, improved;
+    uint32_t att, succ;
+    uint32_t xlogu, xrand, xlevel, xpos;
+    uint32_t icm, icm_team_bytes;
+    uint32_t misc;
+    int32_t stage_adj;
+    int32_t teams;              // ICM teams (warps, or one block-wide team)
+    int32_t max_n_pad, max_kmax, max_R, max_nt;
+};
+
+// Trace of every random decision of the reference's sequential algorithm,
+// consumed by the replay variant of the kernel.
+struct ReplayArgs {
+    const double* uniforms;         // sweep uniforms, (step, sweep, replica) order
+    const uint64_t* sweep_offsets;  // pts*sweeps*R + 1
+    const int32_t* xchg_slot;       // pts * chains*(nt-1)
+    const double* xchg_logu;
+    const int64_t* icm_seed;        // pts * nc (original site or -1)
+    uint64_t n_uniforms, n_xchg, n_icm;
+};
+
+struct EngineArgs {
+    const InstanceDesc* desc;
+    const int32_t* block_inst;    // block -> instance
+    int32_t n_inst;
+    int32_t n_blocks;
+    // graph pools
+    const int32_t* row;
+    const uint32_t* adj;
+    const int32_t* col;
+    const int32_t* hpool;
+    const double* beta;
+    const uint32_t* thr;
+    const double* ptab;
+    const int32_t* perm;
+    // replica pools
+    int8_t* spins;                // master copy
+    int32_t* fields;
+    long long* energy;
+    int8_t* spins_pub;            // 2 halves, parity of the PT step
+    long long spins_pub_half;     // elements per half
+    long long* energy_pub;        // 2 * total replicas
+    long long energy_pub_half;
+    unsigned long long* flips;
+    long long* best_E;
+    unsigned long long* best_sweep;
+    int8_t* best_state;
+    // per-instance PT bookkeeping (instance-local replica ids, slot = chain*nt + k)
+    uint32_t* slot_rep;           // total replicas
+    uint32_t* xorder;             // per instance nt entries (at rep_off)
+    uint32_t* xcursor;            // per instance
+    unsigned long long* attempts; // per slot
+    unsigned long long* successes;
+    unsigned int* bar;            // 2 words per instance
+    int* abort_flag;
+    DevStatus* status;
+    // run control
+    unsigned long long step0;
+    int32_t nsteps;
+    int32_t sweeps;
+    int32_t phase_mask;           // 1 sweep, 2 exchange, 4 ICM
+    int32_t flags;                // ENGINE_* flags
+    unsigned long long seed;
+    SmemPlan sm;
+    ReplayArgs replay;
+};
+
+enum EngineFlags : int32_t {
+    ENGINE_BEST_PER_PHASE = 1,    // track the best state after every colour phase
+    ENGINE_REPLAY = 2,            // sequential sweep + traced decisions
+    ENGINE_EXCHANGE_EVEN_ODD = 4, // deterministic even/odd exchange rounds
+};
+
+enum PhaseBits : int32_t { PHASE_SWEEP = 1, PHASE_EXCHANGE = 2, PHASE_ICM = 4 };
+
+}  // namespace pticm

@@ -1,0 +1,795 @@
+// runtime.cu -- host runtime and C ABI of the PT-ICM engine (include/pticm.h).
+//
+// A pticm_ctx is the GPU-resident equivalent of the reference's PTWorker
+// (include/mpi_defs.hh:33-65) for one problem: every replica, the
+// temperature ladder, the slot->replica map (beta_indices), exchange
+// statistics and best-state tracking live in device memory; the host only
+// launches the engine and reads results back.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "pticm.h"
+#include "pticm_engine.h"
+#include "problem_host.h"
+
+namespace pticm {
+cudaError_t launch_engine(const EngineArgs& A, int threads, bool replay, bool block_team, bool cooperative,
+                          cudaStream_t stream);
+cudaError_t engine_max_blocks_per_sm(bool replay, bool block_team, int threads, size_t smem, int* out);
+cudaError_t launch_recompute(const EngineArgs& A, const int32_t* rep_inst, int total_reps, int write_back,
+                             unsigned long long* mismatches, long long* E_out, long long* cut2_out,
+                             cudaStream_t stream);
+cudaError_t launch_init_spins(const EngineArgs& A, const int32_t* rep_inst, int total_reps,
+                              unsigned long long seed, cudaStream_t stream);
+cudaError_t launch_evaluate(const int32_t* row, const uint32_t* adj, const int32_t* h, int n, int n_pad,
+                            const int8_t* states, int count, long long* E_out, long long* cut2_out,
+                            int32_t* dE_out, cudaStream_t stream);
+cudaError_t launch_philox_probe(const uint4* ctr, const uint2* key, uint4* out, int count, cudaStream_t stream);
+}  // namespace pticm
+
+using namespace pticm;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& m) {
+    g_err = m;
+    return code;
+}
+
+#define CK(x)                                                                                    \
+    do {                                                                                         \
+        cudaError_t e_ = (x);                                                                    \
+        if (e_ != cudaSuccess) return fail(PTICM_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+constexpr long long kNoBest = std::numeric_limits<long long>::max();
+constexpr uint32_t kSmemLimit = 232448 - 1024;   // 227 KB opt-in per block, less static smem
+
+template <typename T>
+struct DArr {
+    T* p = nullptr;
+    size_t n = 0;
+    DArr() = default;
+    DArr(const DArr&) = delete;
+    DArr& operator=(const DArr&) = delete;
+    ~DArr() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t alloc(size_t count) {
+        release();
+        n = count;
+        if (count == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) { p = nullptr; n = 0; return e; }
+        return cudaMemset(p, 0, count * sizeof(T));
+    }
+    cudaError_t upload(const std::vector<T>& v, size_t extra = 0) {
+        cudaError_t e = alloc(v.size() + extra);
+        if (e != cudaSuccess || v.empty()) return e;
+        return cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    }
+    cudaError_t download(std::vector<T>& v) const {
+        v.resize(n);
+        if (!n) return cudaSuccess;
+        return cudaMemcpy(v.data(), p, n * sizeof(T), cudaMemcpyDeviceToHost);
+    }
+};
+
+uint32_t align16(uint64_t x) { return (uint32_t)((x + 15) & ~15ull); }
+
+int32_t pad16(int64_t n) { return (int32_t)((n + 15) & ~15ll); }
+
+int check_device() {
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0)
+        return fail(PTICM_ERR_NODEVICE, "no CUDA device is available; the PT-ICM engine has no CPU path");
+    return PTICM_OK;
+}
+
+}  // namespace
+
+struct pticm_problem {
+    HostProblem hp;
+    // device copy for pticm_problem_evaluate
+    DArr<int32_t> d_row, d_h;
+    DArr<uint32_t> d_adj;
+    bool uploaded = false;
+};
+
+struct pticm_ctx {
+    HostProblem P;
+    pticm_opts o{};
+    int nt = 0, C = 2, R = 0, nc = 0;
+    bool ladder_set = false, states_set = false;
+    std::vector<double> beta;
+    InstanceDesc desc{};
+    int rpc = 0, group = 0, threads = 0, teams = 1;
+    bool block_team = false;
+    SmemPlan plan{};
+    uint64_t steps_done = 0, attempts = 0;
+    double last_ms = 0.0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // device pools
+    DArr<InstanceDesc> d_desc;
+    DArr<int32_t> d_block_inst, d_rep_inst, d_row, d_col, d_h, d_perm;
+    DArr<uint32_t> d_adj, d_thr, d_slot, d_order, d_cursor;
+    DArr<double> d_beta, d_ptab;
+    DArr<int8_t> d_spins, d_pub, d_best_state;
+    DArr<int32_t> d_fields;
+    DArr<long long> d_E, d_Epub, d_bestE;
+    DArr<unsigned long long> d_flips, d_bestSweep, d_att, d_succ, d_mismatch;
+    DArr<unsigned int> d_bar;
+    DArr<int> d_abort;
+    DArr<DevStatus> d_status;
+
+    ~pticm_ctx() {
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+// Shared-memory layout for a launch; every region starts on 16 bytes.
+SmemPlan make_plan(const InstanceDesc& D, bool replay, int teams, int threads, bool stage_adj) {
+    SmemPlan S{};
+    uint64_t off = 0;
+    auto take = [&](uint64_t bytes) {
+        const uint32_t o = (uint32_t)off;
+        off = align16(off + bytes);
+        return o;
+    };
+    const int kst = D.kmax + 1, m = std::max(D.nt - 1, 1);
+    S.mbar = take(16);
+    S.stage_adj = stage_adj ? 1 : 0;
+    if (stage_adj) {
+        S.row = take(align16((uint64_t)(D.n + 1) * 4));
+        S.adj = take(align16((uint64_t)D.nnz * 4));
+    }
+    S.col = take((uint64_t)(D.ncolors + 1) * 4);
+    S.h = take((uint64_t)D.n * 4);
+    S.spin = take((uint64_t)D.rpc * D.n_pad);
+    S.field = take((uint64_t)D.rpc * D.n_pad * 4);
+    S.thr = take((uint64_t)D.nt * kst * 4);
+    S.ptab = take(replay ? (uint64_t)D.nt * kst * 8 : 0);
+    S.slot = take((uint64_t)D.R * 4);
+    S.rslot = take((uint64_t)D.rpc * 8);
+    S.order = take((uint64_t)D.nt * 4);
+    S.beta = take((uint64_t)D.nt * 8);
+    S.dbeta = take((uint64_t)D.nt * 8);
+    S.E = take((uint64_t)D.R * 8);
+    S.dEp = take((uint64_t)D.rpc * 4);
+    S.flp = take((uint64_t)D.rpc * 4);
+    S.bestE = take((uint64_t)D.rpc * 8);
+    S.flips = take((uint64_t)D.rpc * 8);
+    S.improved = take((uint64_t)D.rpc * 4);
+    S.att = take((uint64_t)D.R * 4);
+    S.succ = take((uint64_t)D.R * 4);
+    S.xlogu = take((uint64_t)D.chains * m * 4 + 16);
+    S.xrand = take((uint64_t)D.chains * m * 4 + 16);
+    S.xlevel = take((uint64_t)D.nt * 4);
+    S.xpos = take((uint64_t)D.nt * 4);
+    S.icm_team_bytes = align16((uint64_t)D.n_pad * 4 + D.n_pad);
+    S.teams = teams;
+    S.icm = take((uint64_t)teams * S.icm_team_bytes);
+    S.misc = take(512);
+    S.total = (uint32_t)off;
+    S.max_n_pad = D.n_pad;
+    S.max_kmax = D.kmax;
+    S.max_R = D.R;
+    S.max_nt = D.nt;
+    (void)threads;
+    return S;
+}
+
+// Choose replicas per block, block size, ICM teams and the smem plan.
+int configure(pticm_ctx* c, bool replay) {
+    InstanceDesc& D = c->desc;
+    const int R = c->R, n = (int)c->P.n;
+    const int npairs = c->nc * (c->C / 2);
+    int max_class = 1;
+    for (int k = 0; k < c->P.ncolors; k++)
+        max_class = std::max(max_class, c->P.color_off[k + 1] - c->P.color_off[k]);
+    auto fits = [&](int rpc, int threads, int teams, bool stage, SmemPlan& out) {
+        InstanceDesc t = D;
+        t.rpc = rpc;
+        t.group = R / rpc;
+        out = make_plan(t, replay, teams, threads, stage);
+        return out.total <= kSmemLimit;
+    };
+    int rpc = (int)c->o.replicas_per_block;
+    if (replay) rpc = R;
+    if (rpc <= 0) {
+        // one block per instance when the whole run is about one SM of work,
+        // otherwise one replica per block across the GPU
+        SmemPlan tmp;
+        const bool one_block_fits = fits(R, 1024, std::min(32, std::max(1, npairs)), false, tmp);
+        rpc = (one_block_fits && (int64_t)R * n <= 32768) ? R : 1;
+    }
+    if (rpc <= 0 || R % rpc != 0) return fail(PTICM_ERR_INVALID, "replicas_per_block must divide the replica count");
+    const int group = R / rpc;
+    int threads = (int)c->o.block_threads;
+    if (replay) threads = std::min(1024, 32 * std::max(1, std::min(R, 32)));
+    if (threads <= 0) {
+        if (rpc > 1) threads = 1024;
+        else threads = std::min(1024, std::max(128, ((max_class * rpc + 31) / 32) * 32));
+    }
+    if (threads % 32 != 0 || threads > 1024) return fail(PTICM_ERR_INVALID, "block_threads must be a multiple of 32, at most 1024");
+    const bool block_team = (rpc == 1) && !replay;
+    int teams = block_team ? 1 : std::max(1, std::min(threads / 32, std::max(1, npairs)));
+    SmemPlan plan;
+    bool stage = true;
+    while (!fits(rpc, threads, teams, stage, plan)) {
+        if (stage) { stage = false; continue; }
+        if (teams > 1) { teams = std::max(1, teams / 2); continue; }
+        return fail(PTICM_ERR_UNSUPPORTED, "the replicas of one block do not fit in shared memory; use fewer replicas per block");
+    }
+    D.rpc = rpc;
+    D.group = group;
+    c->rpc = rpc;
+    c->group = group;
+    c->threads = threads;
+    c->teams = teams;
+    c->block_team = block_team;
+    c->plan = plan;
+    if (group > 1) {
+        int dev = 0, sms = 0, per_sm = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        CK(engine_max_blocks_per_sm(replay, block_team, threads, plan.total, &per_sm));
+        if ((int64_t)per_sm * sms < group)
+            return fail(PTICM_ERR_UNSUPPORTED, "the replica blocks of one instance cannot all be resident (" +
+                                                   std::to_string(group) + " blocks, " + std::to_string(per_sm * sms) +
+                                                   " resident); raise replicas_per_block");
+    }
+    std::vector<int32_t> bi(group, 0);
+    CK(c->d_block_inst.upload(bi));
+    CK(c->d_desc.upload(std::vector<InstanceDesc>{D}));
+    return PTICM_OK;
+}
+
+EngineArgs make_args(pticm_ctx* c) {
+    EngineArgs A{};
+    A.desc = c->d_desc.p;
+    A.block_inst = c->d_block_inst.p;
+    A.n_inst = 1;
+    A.n_blocks = c->group;
+    A.row = c->d_row.p;
+    A.adj = c->d_adj.p;
+    A.col = c->d_col.p;
+    A.hpool = c->d_h.p;
+    A.beta = c->d_beta.p;
+    A.thr = c->d_thr.p;
+    A.ptab = c->d_ptab.p;
+    A.perm = c->d_perm.p;
+    A.spins = c->d_spins.p;
+    A.fields = c->d_fields.p;
+    A.energy = c->d_E.p;
+    A.spins_pub = c->d_pub.p;
+    A.spins_pub_half = (long long)c->R * c->desc.n_pad;
+    A.energy_pub = c->d_Epub.p;
+    A.energy_pub_half = c->R;
+    A.flips = c->d_flips.p;
+    A.best_E = c->d_bestE.p;
+    A.best_sweep = c->d_bestSweep.p;
+    A.best_state = c->d_best_state.p;
+    A.slot_rep = c->d_slot.p;
+    A.xorder = c->d_order.p;
+    A.xcursor = c->d_cursor.p;
+    A.attempts = c->d_att.p;
+    A.successes = c->d_succ.p;
+    A.bar = c->d_bar.p;
+    A.abort_flag = c->d_abort.p;
+    A.status = c->d_status.p;
+    A.sweeps = (int)c->o.sweeps;
+    A.seed = c->o.seed;
+    A.sm = c->plan;
+    A.flags = (c->o.best_per_phase ? ENGINE_BEST_PER_PHASE : 0) | (c->o.exchange == 1 ? ENGINE_EXCHANGE_EVEN_ODD : 0);
+    return A;
+}
+
+int read_status(pticm_ctx* c, const char* what) {
+    DevStatus st{};
+    CK(cudaMemcpy(&st, c->d_status.p, sizeof(st), cudaMemcpyDeviceToHost));
+    if (st.error) {
+        static const char* names[] = {"ok", "group barrier wait expired", "bulk-copy wait expired",
+                                      "union-find retry cap", "replay trace mismatch", "index out of range",
+                                      "aborted"};
+        const char* nm = (st.error >= 0 && st.error <= 6) ? names[st.error] : "unknown";
+        return fail(PTICM_ERR_DEVICE, std::string(what) + ": device reported " + nm + " at site " +
+                                          std::to_string(st.where) + " (" + std::to_string(st.aux0) + ", " +
+                                          std::to_string(st.aux1) + ")");
+    }
+    return PTICM_OK;
+}
+
+int reset_flags(pticm_ctx* c) {
+    CK(cudaMemsetAsync(c->d_bar.p, 0, c->d_bar.n * sizeof(unsigned), c->stream));
+    CK(cudaMemsetAsync(c->d_abort.p, 0, sizeof(int), c->stream));
+    CK(cudaMemsetAsync(c->d_status.p, 0, sizeof(DevStatus), c->stream));
+    return PTICM_OK;
+}
+
+// Fresh bookkeeping after new spins: fields/energies from scratch, best =
+// initial state with energy "none yet", identity slot map, shuffled order.
+int reset_run_state(pticm_ctx* c) {
+    EngineArgs A = make_args(c);
+    CK(launch_recompute(A, c->d_rep_inst.p, c->R, 1, nullptr, nullptr, nullptr, c->stream));
+    std::vector<long long> be(c->R, kNoBest);
+    CK(cudaMemcpyAsync(c->d_bestE.p, be.data(), be.size() * sizeof(long long), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_best_state.p, c->d_spins.p, c->d_spins.n, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemsetAsync(c->d_bestSweep.p, 0, c->R * sizeof(unsigned long long), c->stream));
+    CK(cudaMemsetAsync(c->d_flips.p, 0, c->R * sizeof(unsigned long long), c->stream));
+    CK(cudaMemsetAsync(c->d_att.p, 0, c->R * sizeof(unsigned long long), c->stream));
+    CK(cudaMemsetAsync(c->d_succ.p, 0, c->R * sizeof(unsigned long long), c->stream));
+    std::vector<uint32_t> slot(c->R);
+    for (int r = 0; r < c->R; r++) slot[r] = (uint32_t)r;
+    CK(cudaMemcpyAsync(c->d_slot.p, slot.data(), slot.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    std::vector<uint32_t> order(std::max(c->nt, 1), 0);
+    for (int k = 0; k + 1 < c->nt; k++) order[k] = (uint32_t)k;
+    std::mt19937_64 g(c->o.seed ^ 0x6F72646572ull);
+    if (c->nt > 2) std::shuffle(order.begin(), order.begin() + (c->nt - 1), g);
+    CK(cudaMemcpyAsync(c->d_order.p, order.data(), order.size() * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->steps_done = 0;
+    c->attempts = 0;
+    c->states_set = true;
+    return PTICM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* pticm_last_error(void) { return g_err.c_str(); }
+
+const char* pticm_version(void) { return "pticm-gb300 0.1 (sm_103a)"; }
+
+int pticm_problem_load_gset(const char* path, pticm_problem** out) {
+    if (!path || !out) return fail(PTICM_ERR_INVALID, "null argument");
+    auto p = std::make_unique<pticm_problem>();
+    std::string msg;
+    int rc = parse_gset(path, p->hp, msg);
+    if (rc) return fail(rc, msg);
+    *out = p.release();
+    return PTICM_OK;
+}
+
+int pticm_problem_from_coo(int64_t n, int64_t m, const int32_t* src, const int32_t* dst, const double* w,
+                           const double* h, pticm_problem** out) {
+    if (!out) return fail(PTICM_ERR_INVALID, "null argument");
+    auto p = std::make_unique<pticm_problem>();
+    std::string msg;
+    int rc = problem_from_coo(n, m, src, dst, w, h, p->hp, msg);
+    if (rc) return fail(rc, msg);
+    *out = p.release();
+    return PTICM_OK;
+}
+
+int pticm_problem_from_dense(int64_t n, const double* J, const double* h, pticm_problem** out) {
+    if (!out) return fail(PTICM_ERR_INVALID, "null argument");
+    auto p = std::make_unique<pticm_problem>();
+    std::string msg;
+    int rc = problem_from_dense(n, J, h, p->hp, msg);
+    if (rc) return fail(rc, msg);
+    *out = p.release();
+    return PTICM_OK;
+}
+
+void pticm_problem_free(pticm_problem* p) { delete p; }
+
+int pticm_problem_get_info(const pticm_problem* p, pticm_problem_info* out) {
+    if (!p || !out) return fail(PTICM_ERR_INVALID, "null argument");
+    const HostProblem& P = p->hp;
+    out->n = P.n;
+    out->m = P.m;
+    out->nnz = (int64_t)P.col.size();
+    out->sparse = P.sparse ? 1 : 0;
+    out->ncolors = P.ncolors;
+    out->kmax = P.kmax;
+    out->has_linear = P.has_h ? 1 : 0;
+    out->char_scale = P.char_scale;
+    out->total_weight = P.total_weight;
+    return PTICM_OK;
+}
+
+int pticm_problem_evaluate(const pticm_problem* pc, int64_t count, const uint8_t* states, double* energy,
+                           double* maxcut, double* dE) {
+    if (!pc || count < 0 || (count > 0 && !states)) return fail(PTICM_ERR_INVALID, "invalid arguments");
+    if (int rc = check_device()) return rc;
+    if (count == 0) return PTICM_OK;
+    pticm_problem* p = const_cast<pticm_problem*>(pc);
+    const HostProblem& P = p->hp;
+    const int n = (int)P.n, npad = pad16(n);
+    if (!p->uploaded) {
+        CK(p->d_row.upload(P.drow, 4));
+        CK(p->d_adj.upload(P.dadj, 4));
+        CK(p->d_h.upload(P.dh, 4));
+        p->uploaded = true;
+    }
+    std::vector<int8_t> dev((size_t)count * npad, 1);
+    for (int64_t g = 0; g < count; g++)
+        for (int i = 0; i < n; i++) dev[g * npad + i] = states[g * n + P.perm[i]] ? 1 : -1;
+    DArr<int8_t> d_s;
+    DArr<long long> d_E, d_c;
+    DArr<int32_t> d_dE;
+    CK(d_s.upload(dev));
+    CK(d_E.alloc(count));
+    CK(d_c.alloc(count));
+    if (dE) CK(d_dE.alloc((size_t)count * npad));
+    CK(launch_evaluate(p->d_row.p, p->d_adj.p, P.has_h ? p->d_h.p : nullptr, n, npad, d_s.p, (int)count, d_E.p,
+                       d_c.p, dE ? d_dE.p : nullptr, nullptr));
+    CK(cudaDeviceSynchronize());
+    std::vector<long long> E, C2;
+    CK(d_E.download(E));
+    CK(d_c.download(C2));
+    for (int64_t g = 0; g < count; g++) {
+        if (energy) energy[g] = (double)E[g];
+        if (maxcut) maxcut[g] = 0.5 * (double)C2[g];
+    }
+    if (dE) {
+        std::vector<int32_t> d;
+        CK(d_dE.download(d));
+        for (int64_t g = 0; g < count; g++)
+            for (int i = 0; i < n; i++) dE[g * n + P.perm[i]] = (double)d[g * npad + i];
+    }
+    return PTICM_OK;
+}
+
+void pticm_opts_default(pticm_opts* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->seed = 0;
+    o->nt = 20;
+    o->chains = 2;
+    o->sweeps = 1;
+    o->icm = 0;
+    o->exchange = 0;
+    o->best_per_phase = 1;
+}
+
+int pticm_beta_linspace(double* beta, double T0, double T1, uint64_t nt, int inverse) {
+    if (!beta || nt < 2) return fail(PTICM_ERR_INVALID, "need at least two temperatures");
+    beta_linspace(beta, T0, T1, nt, inverse != 0);
+    return PTICM_OK;
+}
+
+int pticm_create(const pticm_problem* p, const pticm_opts* o, pticm_ctx** out) {
+    if (!p || !o || !out) return fail(PTICM_ERR_INVALID, "null argument");
+    if (o->nt < 2) return fail(PTICM_ERR_INVALID, "at least two temperatures are needed");
+    if (o->chains < 1 || o->chains > 16) return fail(PTICM_ERR_INVALID, "chains must be in [1, 16]");
+    if (o->icm && (o->chains % 2)) return fail(PTICM_ERR_INVALID, "ICM pairs chains: use an even chain count");
+    if (o->sweeps < 1) return fail(PTICM_ERR_INVALID, "sweeps must be >= 1");
+    if (int rc = check_device()) return rc;
+    auto c = std::make_unique<pticm_ctx>();
+    c->P = p->hp;
+    c->o = *o;
+    c->nt = (int)o->nt;
+    c->C = (int)o->chains;
+    c->R = c->nt * c->C;
+    const HostProblem& P = c->P;
+    InstanceDesc& D = c->desc;
+    D.n = (int32_t)P.n;
+    D.n_pad = pad16(P.n);
+    D.nnz = (int32_t)P.dadj.size();
+    D.ncolors = P.ncolors;
+    D.kmax = P.kmax;
+    D.nt = c->nt;
+    D.chains = c->C;
+    D.R = c->R;
+    D.nc = 0;
+    D.has_h = P.has_h ? 1 : 0;
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&c->ev0));
+    CK(cudaEventCreate(&c->ev1));
+    CK(c->d_row.upload(P.drow, 4));
+    CK(c->d_adj.upload(P.dadj, 4));
+    CK(c->d_col.upload(P.color_off, 4));
+    CK(c->d_h.upload(P.dh, 4));
+    CK(c->d_perm.upload(P.perm, 4));
+    const size_t spins = (size_t)c->R * D.n_pad;
+    CK(c->d_spins.alloc(spins));
+    CK(c->d_fields.alloc(spins));
+    CK(c->d_best_state.alloc(spins));
+    CK(c->d_pub.alloc(2 * spins));
+    CK(c->d_E.alloc(c->R));
+    CK(c->d_Epub.alloc(2 * c->R));
+    CK(c->d_bestE.alloc(c->R));
+    CK(c->d_flips.alloc(c->R));
+    CK(c->d_bestSweep.alloc(c->R));
+    CK(c->d_att.alloc(c->R));
+    CK(c->d_succ.alloc(c->R));
+    CK(c->d_slot.alloc(c->R));
+    CK(c->d_order.alloc(std::max(c->nt, 1)));
+    CK(c->d_cursor.alloc(1));
+    CK(c->d_bar.alloc(2));
+    CK(c->d_abort.alloc(1));
+    CK(c->d_status.alloc(1));
+    CK(c->d_mismatch.alloc(1));
+    std::vector<int32_t> ri(c->R, 0);
+    CK(c->d_rep_inst.upload(ri));
+    CK(c->d_desc.upload(std::vector<InstanceDesc>{D}));
+    *out = c.release();
+    return PTICM_OK;
+}
+
+void pticm_destroy(pticm_ctx* c) { delete c; }
+
+int pticm_set_ladder(pticm_ctx* c, const double* beta, uint32_t nt, int32_t nc) {
+    if (!c || !beta) return fail(PTICM_ERR_INVALID, "null argument");
+    if ((int)nt != c->nt) return fail(PTICM_ERR_INVALID, "ladder length differs from the context's nt");
+    for (uint32_t k = 0; k < nt; k++)
+        if (!std::isfinite(beta[k])) return fail(PTICM_ERR_INVALID, "non-finite inverse temperature");
+    c->beta.assign(beta, beta + nt);
+    int count = 0;
+    if (nc >= 0) {
+        count = std::min<int>(nc, c->nt);
+    } else {
+        for (int i = c->nt - 1; i >= 0; i--) {
+            if (c->beta[i] < c->P.char_scale) break;
+            count++;
+        }
+    }
+    c->nc = (c->o.icm && c->C >= 2) ? count : 0;
+    c->desc.nc = c->nc;
+    const int kst = c->P.kmax + 1;
+    std::vector<uint32_t> thr((size_t)c->nt * kst, 0xFFFFFFFFu);
+    std::vector<double> ptab((size_t)c->nt * kst, 1.0);
+    for (int k = 0; k < c->nt; k++)
+        for (int t = 1; t < kst; t++) {
+            const double dE = 2.0 * t;
+            const double p = std::exp(-c->beta[k] * dE);   // the reference's expression, src/replica.cc:35
+            ptab[(size_t)k * kst + t] = p;
+            const double scaled = std::ceil(p * 4294967296.0);
+            thr[(size_t)k * kst + t] = (p >= 1.0 || scaled >= 4294967295.0) ? 0xFFFFFFFFu : (uint32_t)scaled;
+        }
+    CK(c->d_beta.upload(c->beta));
+    CK(c->d_thr.upload(thr, 4));
+    CK(c->d_ptab.upload(ptab, 4));
+    c->ladder_set = true;
+    return PTICM_OK;
+}
+
+int pticm_set_states(pticm_ctx* c, const uint8_t* states) {
+    if (!c || !states) return fail(PTICM_ERR_INVALID, "null argument");
+    const HostProblem& P = c->P;
+    const int n = (int)P.n, npad = c->desc.n_pad;
+    std::vector<int8_t> dev((size_t)c->R * npad, 1);
+    for (int r = 0; r < c->R; r++)
+        for (int i = 0; i < n; i++) dev[(size_t)r * npad + i] = states[(size_t)r * n + P.perm[i]] ? 1 : -1;
+    CK(cudaMemcpy(c->d_spins.p, dev.data(), dev.size(), cudaMemcpyHostToDevice));
+    if (int rc = configure(c, false)) return rc;
+    return reset_run_state(c);
+}
+
+int pticm_init_states(pticm_ctx* c, uint64_t seed) {
+    if (!c) return fail(PTICM_ERR_INVALID, "null argument");
+    if (int rc = configure(c, false)) return rc;
+    EngineArgs A = make_args(c);
+    CK(launch_init_spins(A, c->d_rep_inst.p, c->R, seed, c->stream));
+    return reset_run_state(c);
+}
+
+int pticm_run(pticm_ctx* c, uint64_t pt_steps, uint32_t phase_mask) {
+    if (!c) return fail(PTICM_ERR_INVALID, "null argument");
+    if (!c->ladder_set) return fail(PTICM_ERR_INVALID, "set a ladder before running");
+    if (!c->states_set) return fail(PTICM_ERR_INVALID, "initialise the replica states before running");
+    if (phase_mask == 0 || phase_mask > 7) return fail(PTICM_ERR_INVALID, "phase_mask must be in 1..7");
+    if (int rc = configure(c, false)) return rc;
+    c->last_ms = 0.0;
+    uint64_t left = pt_steps;
+    while (left > 0) {
+        const int chunk = (int)std::min<uint64_t>(left, 1u << 16);
+        if (int rc = reset_flags(c)) return rc;
+        EngineArgs A = make_args(c);
+        A.step0 = c->steps_done;
+        A.nsteps = chunk;
+        A.phase_mask = (int)phase_mask;
+        CK(cudaEventRecord(c->ev0, c->stream));
+        CK(launch_engine(A, c->threads, false, c->block_team, c->group > 1, c->stream));
+        CK(cudaEventRecord(c->ev1, c->stream));
+        CK(cudaEventSynchronize(c->ev1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+        c->last_ms += ms;
+        if (int rc = read_status(c, "pticm_run")) return rc;
+        c->steps_done += (uint64_t)chunk;
+        if (phase_mask & PHASE_SWEEP) c->attempts += (uint64_t)chunk * c->o.sweeps * (uint64_t)c->R * (uint64_t)c->P.n;
+        left -= (uint64_t)chunk;
+    }
+    return PTICM_OK;
+}
+
+int pticm_replay(pticm_ctx* c, const pticm_trace* t) {
+    if (!c || !t) return fail(PTICM_ERR_INVALID, "null argument");
+    if (c->C != 2) return fail(PTICM_ERR_INVALID, "replay follows the reference: two chains");
+    if (!c->ladder_set || !c->states_set) return fail(PTICM_ERR_INVALID, "set the ladder and the states first");
+    for (int k = 0; k + 1 < c->nt; k++)
+        for (int j = k + 1; j < c->nt; j++)
+            if (std::fabs(c->beta[k] - c->beta[j]) < 1e-10)
+                return fail(PTICM_ERR_UNSUPPORTED, "replay needs distinct temperatures");
+    if (int rc = configure(c, true)) return rc;
+    const uint64_t steps = t->pt_steps;
+    const uint64_t nsw = steps * c->o.sweeps * (uint64_t)c->R;
+    DArr<double> d_u, d_logu;
+    DArr<uint64_t> d_off;
+    DArr<int32_t> d_xs;
+    DArr<int64_t> d_seed;
+    std::vector<double> u(t->uniforms, t->uniforms + t->n_uniforms);
+    std::vector<uint64_t> off(t->sweep_offsets, t->sweep_offsets + nsw + 1);
+    const uint64_t nx = steps * 2 * (uint64_t)(c->nt - 1);
+    std::vector<int32_t> xs(t->xchg_slot, t->xchg_slot + nx);
+    std::vector<double> xl(t->xchg_logu, t->xchg_logu + nx);
+    const uint64_t ni = steps * (uint64_t)c->nc;
+    std::vector<int64_t> seeds;
+    if (ni) seeds.assign(t->icm_seed, t->icm_seed + ni);
+    CK(d_u.upload(u, 1));
+    CK(d_off.upload(off));
+    CK(d_xs.upload(xs, 1));
+    CK(d_logu.upload(xl, 1));
+    CK(d_seed.upload(seeds, 1));
+    if (int rc = reset_flags(c)) return rc;
+    EngineArgs A = make_args(c);
+    A.step0 = c->steps_done;
+    A.nsteps = (int)steps;
+    A.phase_mask = PHASE_SWEEP | PHASE_EXCHANGE | (c->nc ? PHASE_ICM : 0);
+    A.flags = ENGINE_REPLAY;
+    A.replay.uniforms = d_u.p;
+    A.replay.sweep_offsets = reinterpret_cast<const uint64_t*>(d_off.p);
+    A.replay.xchg_slot = d_xs.p;
+    A.replay.xchg_logu = d_logu.p;
+    A.replay.icm_seed = reinterpret_cast<const int64_t*>(d_seed.p);
+    A.replay.n_uniforms = u.size();
+    A.replay.n_xchg = xs.size();
+    A.replay.n_icm = seeds.size();
+    CK(cudaEventRecord(c->ev0, c->stream));
+    CK(launch_engine(A, c->threads, true, false, false, c->stream));
+    CK(cudaEventRecord(c->ev1, c->stream));
+    CK(cudaEventSynchronize(c->ev1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    c->last_ms = ms;
+    if (int rc = read_status(c, "pticm_replay")) return rc;
+    c->steps_done += steps;
+    c->attempts += steps * c->o.sweeps * (uint64_t)c->R * (uint64_t)c->P.n;
+    return PTICM_OK;
+}
+
+int pticm_get_stats(pticm_ctx* c, pticm_stats* s, uint64_t* swap_attempts, uint64_t* swap_successes) {
+    if (!c) return fail(PTICM_ERR_INVALID, "null argument");
+    CK(cudaStreamSynchronize(c->stream));
+    std::vector<unsigned long long> fl, at, su;
+    CK(c->d_flips.download(fl));
+    CK(c->d_att.download(at));
+    CK(c->d_succ.download(su));
+    if (s) {
+        s->pt_steps = c->steps_done;
+        s->attempts = c->attempts;
+        s->flips = 0;
+        for (auto v : fl) s->flips += v;
+        s->swaps = 0;
+        for (auto v : su) s->swaps += v;
+        s->nt = (uint32_t)c->nt;
+        s->chains = (uint32_t)c->C;
+        s->nc = (uint32_t)c->nc;
+        s->replicas = (uint32_t)c->R;
+        s->last_run_ms = c->last_ms;
+    }
+    for (int k = 0; k < c->R; k++) {
+        if (swap_attempts) swap_attempts[k] = at[k];
+        if (swap_successes) swap_successes[k] = su[k];
+    }
+    return PTICM_OK;
+}
+
+int pticm_get_best(pticm_ctx* c, double* energy, uint64_t* sweep, uint8_t* state, int64_t* replica) {
+    if (!c) return fail(PTICM_ERR_INVALID, "null argument");
+    CK(cudaStreamSynchronize(c->stream));
+    std::vector<long long> be;
+    std::vector<unsigned long long> bs;
+    CK(c->d_bestE.download(be));
+    CK(c->d_bestSweep.download(bs));
+    int64_t bi = -1;
+    long long best = kNoBest;
+    for (int r = 0; r < c->R; r++)
+        if (be[r] < best) { best = be[r]; bi = r; }
+    if (energy) *energy = (bi < 0) ? DBL_MAX : (double)best;
+    if (sweep) *sweep = (bi < 0) ? 0 : bs[bi];
+    if (replica) *replica = bi;
+    if (state) {
+        const int n = (int)c->P.n, npad = c->desc.n_pad;
+        std::vector<int8_t> row(npad, 1);
+        if (bi >= 0) CK(cudaMemcpy(row.data(), c->d_best_state.p + (size_t)bi * npad, npad, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < n; i++) state[c->P.perm[i]] = row[i] > 0 ? 1 : 0;
+    }
+    return PTICM_OK;
+}
+
+int pticm_get_replicas(pticm_ctx* c, uint8_t* states, int64_t* energy, int32_t* fields, uint32_t* slot_of_replica) {
+    if (!c) return fail(PTICM_ERR_INVALID, "null argument");
+    CK(cudaStreamSynchronize(c->stream));
+    const int n = (int)c->P.n, npad = c->desc.n_pad;
+    if (states) {
+        std::vector<int8_t> s;
+        CK(c->d_spins.download(s));
+        for (int r = 0; r < c->R; r++)
+            for (int i = 0; i < n; i++) states[(size_t)r * n + c->P.perm[i]] = s[(size_t)r * npad + i] > 0 ? 1 : 0;
+    }
+    if (fields) {
+        std::vector<int32_t> f;
+        CK(c->d_fields.download(f));
+        for (int r = 0; r < c->R; r++)
+            for (int i = 0; i < n; i++) fields[(size_t)r * n + c->P.perm[i]] = f[(size_t)r * npad + i];
+    }
+    if (energy) {
+        std::vector<long long> e;
+        CK(c->d_E.download(e));
+        for (int r = 0; r < c->R; r++) energy[r] = e[r];
+    }
+    if (slot_of_replica) {
+        std::vector<uint32_t> sl;
+        CK(c->d_slot.download(sl));
+        for (int s = 0; s < c->R; s++) slot_of_replica[sl[s]] = (uint32_t)s;
+    }
+    return PTICM_OK;
+}
+
+int pticm_get_ladder(pticm_ctx* c, double* beta, uint32_t* slot_to_replica, uint32_t* nc) {
+    if (!c) return fail(PTICM_ERR_INVALID, "null argument");
+    if (beta) for (int k = 0; k < c->nt; k++) beta[k] = c->beta.empty() ? 0.0 : c->beta[k];
+    if (nc) *nc = (uint32_t)c->nc;
+    if (slot_to_replica) {
+        CK(cudaStreamSynchronize(c->stream));
+        std::vector<uint32_t> sl;
+        CK(c->d_slot.download(sl));
+        for (int s = 0; s < c->R; s++) slot_to_replica[s] = sl[s];
+    }
+    return PTICM_OK;
+}
+
+int pticm_verify(pticm_ctx* c, uint64_t* mismatches) {
+    if (!c || !mismatches) return fail(PTICM_ERR_INVALID, "null argument");
+    if (!c->states_set) return fail(PTICM_ERR_INVALID, "no states yet");
+    CK(cudaMemsetAsync(c->d_mismatch.p, 0, sizeof(unsigned long long), c->stream));
+    EngineArgs A = make_args(c);
+    CK(launch_recompute(A, c->d_rep_inst.p, c->R, 0, c->d_mismatch.p, nullptr, nullptr, c->stream));
+    unsigned long long mm = 0;
+    CK(cudaMemcpyAsync(&mm, c->d_mismatch.p, sizeof(mm), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    *mismatches = mm;
+    return PTICM_OK;
+}
+
+int pticm_philox_probe(const uint32_t* ctr, const uint32_t* key, uint32_t* out, int count) {
+    if (!ctr || !key || !out || count <= 0) return fail(PTICM_ERR_INVALID, "invalid arguments");
+    if (int rc = check_device()) return rc;
+    DArr<uint4> dc, dout;
+    DArr<uint2> dk;
+    CK(dc.alloc(count));
+    CK(dk.alloc(count));
+    CK(dout.alloc(count));
+    CK(cudaMemcpy(dc.p, ctr, (size_t)count * 16, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dk.p, key, (size_t)count * 8, cudaMemcpyHostToDevice));
+    CK(launch_philox_probe(dc.p, dk.p, dout.p, count, nullptr));
+    CK(cudaMemcpy(out, dout.p, (size_t)count * 16, cudaMemcpyDeviceToHost));
+    return PTICM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,282 @@
+"""Python binding of the GB300 PT-ICM engine (include/pticm.h) over ctypes.
+
+The names mirror the reference's libreplica interface: `Problem` is
+pticm::Problem (src/problem.cc), `Context` is the PTWorker state that
+`solve` drives (src/solver.cc), and `solve()` runs the whole PT-ICM loop
+and returns the keys the reference prints (src/solver.cc:151-163).
+
+There is no CPU path: every call goes to libpticm_gb300.so, which needs a
+CUDA device; loading fails loudly when the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libpticm_gb300.so")
+
+PHASE_SWEEP, PHASE_EXCHANGE, PHASE_ICM = 1, 2, 4
+PHASE_ALL = 7
+
+
+class PticmError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"pticm error {code}: {msg}")
+        self.code = code
+
+
+class ProblemInfo(C.Structure):
+    _fields_ = [("n", C.c_int64), ("m", C.c_int64), ("nnz", C.c_int64), ("sparse", C.c_int32),
+                ("ncolors", C.c_int32), ("kmax", C.c_int32), ("has_linear", C.c_int32),
+                ("char_scale", C.c_double), ("total_weight", C.c_double)]
+
+
+class Opts(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("nt", C.c_uint32), ("chains", C.c_uint32), ("sweeps", C.c_uint32),
+                ("icm", C.c_uint32), ("exchange", C.c_uint32), ("best_per_phase", C.c_uint32),
+                ("block_threads", C.c_uint32), ("replicas_per_block", C.c_uint32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("pt_steps", C.c_uint64), ("attempts", C.c_uint64), ("flips", C.c_uint64),
+                ("swaps", C.c_uint64), ("nt", C.c_uint32), ("chains", C.c_uint32), ("nc", C.c_uint32),
+                ("replicas", C.c_uint32), ("last_run_ms", C.c_double)]
+
+
+class Trace(C.Structure):
+    _fields_ = [("pt_steps", C.c_uint64), ("uniforms", C.c_void_p), ("n_uniforms", C.c_uint64),
+                ("sweep_offsets", C.c_void_p), ("xchg_slot", C.c_void_p), ("xchg_logu", C.c_void_p),
+                ("icm_seed", C.c_void_p)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libpticm_gb300.so (build it with __graft_entry__.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build the native library first "
+                           "(python -c 'import __graft_entry__ as g; g.build()')")
+    L = C.CDLL(LIB_PATH)
+    P = C.c_void_p
+    i64, u64, u32, i32, dbl = C.c_int64, C.c_uint64, C.c_uint32, C.c_int32, C.c_double
+    sigs = {
+        "pticm_problem_load_gset": [C.c_char_p, C.POINTER(P)],
+        "pticm_problem_from_coo": [i64, i64, P, P, P, P, C.POINTER(P)],
+        "pticm_problem_from_dense": [i64, P, P, C.POINTER(P)],
+        "pticm_problem_get_info": [P, C.POINTER(ProblemInfo)],
+        "pticm_problem_evaluate": [P, i64, P, P, P, P],
+        "pticm_create": [P, C.POINTER(Opts), C.POINTER(P)],
+        "pticm_set_ladder": [P, P, u32, i32],
+        "pticm_beta_linspace": [P, dbl, dbl, u64, C.c_int],
+        "pticm_init_states": [P, u64],
+        "pticm_set_states": [P, P],
+        "pticm_run": [P, u64, u32],
+        "pticm_get_stats": [P, C.POINTER(Stats), P, P],
+        "pticm_get_best": [P, P, P, P, P],
+        "pticm_get_replicas": [P, P, P, P, P],
+        "pticm_get_ladder": [P, P, P, P],
+        "pticm_verify": [P, P],
+        "pticm_replay": [P, C.POINTER(Trace)],
+        "pticm_philox_probe": [P, P, P, C.c_int],
+    }
+    for name, args in sigs.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    L.pticm_problem_free.argtypes = [P]
+    L.pticm_problem_free.restype = None
+    L.pticm_destroy.argtypes = [P]
+    L.pticm_destroy.restype = None
+    L.pticm_opts_default.argtypes = [C.POINTER(Opts)]
+    L.pticm_opts_default.restype = None
+    L.pticm_last_error.restype = C.c_char_p
+    L.pticm_version.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise PticmError(rc, lib().pticm_last_error().decode())
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Problem:
+    """pticm::Problem: Ising couplings J_ij and linear terms h_i."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    @classmethod
+    def load(cls, path: str) -> "Problem":
+        h = C.c_void_p()
+        _check(lib().pticm_problem_load_gset(os.fspath(path).encode(), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_coo(cls, n, src, dst, w, h=None) -> "Problem":
+        src = np.ascontiguousarray(src, np.int32)
+        dst = np.ascontiguousarray(dst, np.int32)
+        w = np.ascontiguousarray(w, np.float64)
+        hh = None if h is None else np.ascontiguousarray(h, np.float64)
+        out = C.c_void_p()
+        _check(lib().pticm_problem_from_coo(n, len(src), _p(src), _p(dst), _p(w), _p(hh), C.byref(out)))
+        return cls(out)
+
+    @classmethod
+    def from_instance(cls, inst) -> "Problem":
+        return cls.from_coo(inst.n, inst.src, inst.dst, inst.w, inst.h)
+
+    @classmethod
+    def from_dense(cls, J, h=None) -> "Problem":
+        J = np.ascontiguousarray(J, np.float64)
+        hh = None if h is None else np.ascontiguousarray(h, np.float64)
+        out = C.c_void_p()
+        _check(lib().pticm_problem_from_dense(J.shape[0], _p(J), _p(hh), C.byref(out)))
+        return cls(out)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.pticm_problem_free(self._h)
+            self._h = None
+
+    def info(self) -> ProblemInfo:
+        inf = ProblemInfo()
+        _check(lib().pticm_problem_get_info(self._h, C.byref(inf)))
+        return inf
+
+    @property
+    def n(self) -> int:
+        return self.info().n
+
+    def evaluate(self, states, with_dE=False):
+        """Energy, max-cut and (optionally) dE of each state (rows of 0/1)."""
+        s = np.ascontiguousarray(np.atleast_2d(states), np.uint8)
+        cnt, n = s.shape
+        E = np.zeros(cnt)
+        cut = np.zeros(cnt)
+        dE = np.zeros((cnt, n)) if with_dE else None
+        _check(lib().pticm_problem_evaluate(self._h, cnt, _p(s), _p(E), _p(cut), _p(dE)))
+        return (E, cut, dE) if with_dE else (E, cut)
+
+
+def beta_linspace(T0, T1, nt, inverse=False):
+    b = np.zeros(nt)
+    _check(lib().pticm_beta_linspace(_p(b), T0, T1, nt, int(inverse)))
+    return b
+
+
+class Context:
+    """All replicas of one PT run resident on the current GPU."""
+
+    def __init__(self, problem: Problem, *, nt, chains=2, seed=0, sweeps=1, icm=True, exchange=0,
+                 best_per_phase=True, block_threads=0, replicas_per_block=0):
+        L = lib()
+        o = Opts()
+        L.pticm_opts_default(C.byref(o))
+        o.seed, o.nt, o.chains, o.sweeps, o.icm = seed, nt, chains, sweeps, int(icm)
+        o.exchange, o.best_per_phase = exchange, int(best_per_phase)
+        o.block_threads, o.replicas_per_block = block_threads, replicas_per_block
+        h = C.c_void_p()
+        _check(L.pticm_create(problem._h, C.byref(o), C.byref(h)))
+        self._h = h
+        self.problem = problem
+        self.nt, self.chains, self.R = nt, chains, nt * chains
+        self.n = problem.n
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.pticm_destroy(self._h)
+            self._h = None
+
+    def set_ladder(self, beta, nc=-1):
+        b = np.ascontiguousarray(beta, np.float64)
+        _check(lib().pticm_set_ladder(self._h, _p(b), len(b), nc))
+
+    def init_states(self, seed):
+        _check(lib().pticm_init_states(self._h, seed))
+
+    def set_states(self, states):
+        s = np.ascontiguousarray(states, np.uint8).reshape(self.R, self.n)
+        _check(lib().pticm_set_states(self._h, _p(s)))
+
+    def run(self, steps, phases=PHASE_ALL):
+        _check(lib().pticm_run(self._h, steps, phases))
+
+    def stats(self):
+        st = Stats()
+        at = np.zeros(self.R, np.uint64)
+        su = np.zeros(self.R, np.uint64)
+        _check(lib().pticm_get_stats(self._h, C.byref(st), _p(at), _p(su)))
+        return st, at, su
+
+    def best(self):
+        E = C.c_double()
+        sw = C.c_uint64()
+        rep = C.c_int64()
+        s = np.zeros(self.n, np.uint8)
+        _check(lib().pticm_get_best(self._h, C.byref(E), C.byref(sw), _p(s), C.byref(rep)))
+        return E.value, sw.value, s, rep.value
+
+    def replicas(self):
+        s = np.zeros((self.R, self.n), np.uint8)
+        E = np.zeros(self.R, np.int64)
+        f = np.zeros((self.R, self.n), np.int32)
+        slot = np.zeros(self.R, np.uint32)
+        _check(lib().pticm_get_replicas(self._h, _p(s), _p(E), _p(f), _p(slot)))
+        return s, E, f, slot
+
+    def ladder(self):
+        b = np.zeros(self.nt)
+        s2r = np.zeros(self.R, np.uint32)
+        nc = C.c_uint32()
+        _check(lib().pticm_get_ladder(self._h, _p(b), _p(s2r), C.byref(nc)))
+        return b, s2r, nc.value
+
+    def verify(self) -> int:
+        mm = C.c_uint64()
+        _check(lib().pticm_verify(self._h, C.byref(mm)))
+        return mm.value
+
+    def replay(self, trace: dict, pt_steps: int):
+        """Run the reference's sequential algorithm from a recorded trace
+        (keys: uniforms, sweep_offsets, xchg_pair, xchg_logu, icm_seed)."""
+        u = np.ascontiguousarray(trace["uniforms"], np.float64)
+        off = np.ascontiguousarray(trace["sweep_offsets"], np.uint64)
+        xs = np.ascontiguousarray(trace["xchg_pair"], np.int32)
+        xl = np.ascontiguousarray(trace["xchg_logu"], np.float64)
+        seeds = np.ascontiguousarray(trace["icm_seed"], np.int64)
+        t = Trace(pt_steps, u.ctypes.data, len(u), off.ctypes.data, xs.ctypes.data, xl.ctypes.data,
+                  seeds.ctypes.data)
+        _check(lib().pticm_replay(self._h, C.byref(t)))
+
+
+def solve(problem: Problem, *, seed, Nt, pts, T0=0.6, T1=2.8, inverse=False, icm=False, sweeps=1,
+          ladder=None, chains=2, exchange=0, **kw):
+    """The reference's solve() (src/solver.cc:16-166) on the GPU: linear-beta
+    ladder (or `ladder`), Bernoulli initial states, `pts` PT steps.  Returns
+    the keys src/solver.cc:151-163 prints."""
+    beta = beta_linspace(T0, T1, Nt, inverse) if ladder is None else np.asarray(ladder, np.float64)
+    ctx = Context(problem, nt=len(beta), chains=chains, seed=seed, sweeps=sweeps, icm=icm,
+                  exchange=exchange, **kw)
+    ctx.set_ladder(beta)
+    ctx.init_states(seed)
+    ctx.run(pts)
+    st, att, suc = ctx.stats()
+    E, sweep, state, rep = ctx.best()
+    Eb, cut = problem.evaluate(state[None, :])
+    rates = np.where(att > 0, suc / np.maximum(att, 1), 0.0)
+    return dict(swap_rates=rates, swap_attempts=att, swap_successes=suc, best_state_energy=float(Eb[0]),
+                best_state_sweep=sweep, best_energy=E, best_maxcut=float(cut[0]), num_of_flips=st.flips,
+                num_of_swaps=st.swaps, best_state=state, beta=beta, attempts=st.attempts,
+                device_ms=st.last_run_ms, context=ctx)

@@ -503,7 +503,7 @@ int pticm_create(const pticm_problem* p, const pticm_opts* o, pticm_ctx** out) {
     CK(c->d_adj.upload(P.dadj, 4));
     CK(c->d_col.upload(P.color_off, 4));
     CK(c->d_h.upload(P.dh, 4));
-    CK(c->d_perm.upload(P.perm, 4));
+    CK(c->d_perm.upload(P.iperm, 4));   // original site -> device site
     const size_t spins = (size_t)c->R * D.n_pad;
     CK(c->d_spins.alloc(spins));
     CK(c->d_fields.alloc(spins));

@@ -153,6 +153,18 @@ int pticm_get_ladder(pticm_ctx* c, double* beta, uint32_t* slot_to_replica, uint
  * differing sites and energies (0 = bit-exact). */
 int pticm_verify(pticm_ctx* c, uint64_t* mismatches);
 
+/* Phase timers (tracing): when enabled, every block of the following
+ * pticm_run calls accumulates clock64 cycles spent in the sweep, the
+ * publish+barrier, the exchange and the ICM phases, and the whole launch,
+ * then ICM split into overlap, seed choice, union, flip and energies, and
+ * the exchange split into draws, dependency levels, attempts and reshuffle
+ * (PTICM_PROFILE_SLOTS values).  pticm_get_profile converts them to
+ * milliseconds at the device's maximum SM clock and reports the mean and
+ * the maximum over blocks; enabling again clears the counters. */
+#define PTICM_PROFILE_SLOTS 14
+int pticm_set_profiling(pticm_ctx* c, int enable);
+int pticm_get_profile(pticm_ctx* c, double* mean_ms, double* max_ms);
+
 /* --------------------------------------------------------------- replay -- */
 /* The reference's sequential algorithm driven by a recorded trace of its
  * random decisions: per PT step, per sweep, per replica the uniforms

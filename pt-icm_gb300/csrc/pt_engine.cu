@@ -34,78 +34,71 @@ __device__ __forceinline__ T* sm_ptr(uint8_t* base, uint32_t off) {
     return reinterpret_cast<T*>(base + off);
 }
 
-// ------------------------------------------------------------ union-find
-// Concurrent union-find in shared memory: roots are hooked larger-under-
-// smaller with CAS (so parent pointers strictly decrease and no cycle can
-// form) and finds halve paths.  Retries are capped.
-__device__ __forceinline__ int uf_find(volatile int* parent, int x) {
-    for (int it = 0; it < (1 << 20); it++) {
-        const int p = parent[x];
-        if (p == x) return x;
-        const int gp = parent[p];
-        if (gp == p) return p;
-        parent[x] = gp;
-        x = gp;
+// Thread-0 phase timers (clock64), enabled by EngineArgs::prof.
+struct Prof {
+    bool on;
+    long long mark, sub;
+    long long c[PROF_PHASES];
+    __device__ __forceinline__ void init(bool enable) {
+        on = enable;
+        mark = sub = enable ? clock64() : 0;
+        for (int q = 0; q < PROF_PHASES; q++) c[q] = 0;
     }
-    return -1;
-}
-
-__device__ __forceinline__ bool uf_unite(int* parent, int a, int b) {
-    volatile int* vp = parent;
-    for (int it = 0; it < (1 << 20); it++) {
-        a = uf_find(vp, a);
-        b = uf_find(vp, b);
-        if (a < 0 || b < 0) return false;
-        if (a == b) return true;
-        if (a < b) { const int t = a; a = b; b = t; }
-        if (atomicCAS(parent + a, a, b) == a) return true;
+    __device__ __forceinline__ void tick(int slot) {
+        if (on) { const long long t = clock64(); c[slot] += t - mark; mark = t; sub = t; }
     }
-    return false;
-}
-
-// ---------------------------------------------------------- team helpers
-// An ICM "team" is either one warp (many pairs per block) or the whole block
-// (one pair per block).  Sums go through a per-team shared scratch word.
-template <bool BLOCK>
-struct Team {
-    int tr, ts;                  // rank and size
-    long long* acc;              // team scratch (shared)
-    int* bcast;                  // team scratch (shared)
-    __device__ __forceinline__ void sync() const {
-        if (BLOCK) __syncthreads(); else __syncwarp();
-    }
-    __device__ __forceinline__ long long sum(long long v) const {
-        if (!BLOCK) {
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            return v;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) *acc = 0;
-        __syncthreads();
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if ((threadIdx.x & 31) == 0) atomicAdd(reinterpret_cast<unsigned long long*>(acc), (unsigned long long)v);
-        __syncthreads();
-        const long long r = *acc;
-        __syncthreads();
-        return r;
+    __device__ __forceinline__ void subtick(int slot) {
+        if (on) { const long long t = clock64(); c[slot] += t - sub; sub = t; }
     }
 };
 
-// Position of the r-th (0-based) set flag among d[0..n); one warp scans.
-__device__ __forceinline__ int select_rth(const uint8_t* d, int n, int r, int lane) {
-    int base = 0;
-    for (int c0 = 0; c0 < n; c0 += 32) {
-        const int i = c0 + lane;
-        const bool bit = (i < n) && d[i];
-        unsigned m = __ballot_sync(0xffffffffu, bit);
-        const int c = __popc(m);
-        if (r < base + c) {
-            for (int t = 0; t < r - base; t++) m &= m - 1;
-            return c0 + __ffs(m) - 1;
-        }
-        base += c;
+// ---------------------------------------------------------- team helpers
+// An ICM "team" is either one warp (many pairs per block) or the whole block
+// (one pair per block).  Block-wide reductions go through shared scratch.
+template <bool BLOCK>
+struct Team {
+    int tr, ts;                  // rank and size
+    long long* acc;              // team scratch (shared, 4 words for a block team)
+    int* ctl;                    // team scratch (shared): BFS queue head and tail
+    __device__ __forceinline__ void sync() const {
+        if (BLOCK) __syncthreads(); else __syncwarp();
     }
-    return -1;
+    // (sum, min, min, sum) over the team
+    __device__ __forceinline__ void reduce(long long& s0, unsigned long long& m1, unsigned long long& m2,
+                                           long long& s3) const {
+        for (int o = 16; o > 0; o >>= 1) {
+            s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+            m1 = min(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+            m2 = min(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+            s3 += __shfl_xor_sync(0xffffffffu, s3, o);
+        }
+        if (!BLOCK) return;
+        unsigned long long* u = reinterpret_cast<unsigned long long*>(acc);
+        __syncthreads();
+        if (threadIdx.x == 0) { u[0] = 0; u[1] = ~0ull; u[2] = ~0ull; u[3] = 0; }
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(u + 0, (unsigned long long)s0);
+            atomicMin(u + 1, m1);
+            atomicMin(u + 2, m2);
+            atomicAdd(u + 3, (unsigned long long)s3);
+        }
+        __syncthreads();
+        s0 = (long long)u[0]; m1 = u[1]; m2 = u[2]; s3 = (long long)u[3];
+        __syncthreads();
+    }
+    __device__ __forceinline__ void sum2(long long& a, long long& b) const {
+        unsigned long long x = ~0ull, y = ~0ull;
+        reduce(a, x, y, b);
+    }
+};
+
+// 64-bit finaliser of splitmix64 (Steele, Lea, Flood, OOPSLA 2014): a
+// bijective mixer giving independent-looking keys for consecutive inputs.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
 }
 
 // Per-block view of the launch.
@@ -123,17 +116,39 @@ struct BlockCtx {
     int32_t* tb;        // threshold row base of each local replica
 };
 
+// ICM team scratch: BFS queue (n ints), overlap flags (n bytes), visited
+// bits; the layout matches icm_team_bytes of the shared-memory plan.
+struct IcmScratch {
+    int* queue;
+    uint8_t* d;
+    uint32_t* vis;
+};
+
+__device__ __forceinline__ IcmScratch icm_scratch(uint8_t* base, int n_pad) {
+    IcmScratch X;
+    X.queue = reinterpret_cast<int*>(base);
+    X.d = base + (size_t)n_pad * 4;
+    X.vis = reinterpret_cast<uint32_t*>(base + (size_t)n_pad * 5);
+    return X;
+}
+
 // ------------------------------------------------------------------ ICM
-// One cluster move on the pair (A, B) = (slot a, slot b) at equal beta.  The
-// team computes the overlap, the reference's global-flip rule (src/icm.cc:
-// 20-28), a seed uniform among differing sites (src/icm.cc:33), the seed's
-// cluster of differing sites by union-find, and flips it in each member held
-// by this block.  Members held elsewhere are read from the published copy
-// and flipped by their own block, which computes the same cluster.
+// One cluster move on the pair (A, B) = (chain 2c, chain 2c+1) at slot k.
+// The team computes the overlap (sites where A and B differ), the
+// reference's global-flip rule (src/icm.cc:20-28: more than n/2 differing
+// sites -> negate A), a seed uniform among differing sites (src/icm.cc:33;
+// here the differing site with the smallest per-site random key, which is
+// uniform), then grows the seed's cluster of differing sites breadth-first
+// (src/icm.cc:37-72 grows it depth-first; the cluster is the same set),
+// flipping each member in both replicas as it is reached.  Fields are
+// updated per flip; energies change by -2 s_u h_u per flipped site plus
+// -2 J s_u s_v per edge to a non-cluster neighbour (equal in A and B), an
+// exact integer update.  Members held by another block are read from the
+// published copy and flipped by their own block, which grows the same set.
 template <bool BLOCK, bool REPLAY>
 __device__ void icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK>& team, int q,
-                         int rA, int rB, unsigned long long step, int ls, int* parent, uint8_t* d,
-                         int where_err) {
+                         int rA, int rB, unsigned long long step, int ls, const IcmScratch& X,
+                         int where_err, Prof& P) {
     const InstanceDesc& D = B.D;
     const int n = D.n, npad = D.n_pad;
     const bool locA = rA >= B.r0 && rA < B.r0 + D.rpc;
@@ -145,27 +160,48 @@ __device__ void icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOC
     int8_t* sB = locB ? B.spin + (rB - B.r0) * npad : nullptr;
     int32_t* fA = locA ? B.field + (rA - B.r0) * npad : nullptr;
     int32_t* fB = locB ? B.field + (rB - B.r0) * npad : nullptr;
+    uint8_t* d = X.d;
+    const int nwords = (n + 31) >> 5;
+    if (threadIdx.x == 0) P.subtick(PROF_ICM_ENERGY);
 
-    long long cl = 0;
+    // overlap, its size, seed candidates among differing and equal sites
+    unsigned long long r64 = 0;
+    if (!REPLAY) {
+        const uint4 rnd = philox4x32_10(make_uint4((uint32_t)q, (uint32_t)D.inst_id, (uint32_t)step,
+                                                   (uint32_t)(step >> 32)), stream_key(A.seed, STREAM_ICM));
+        r64 = ((unsigned long long)rnd.y << 32) | rnd.x;
+    }
+    long long cnt = 0, hs = 0;
+    unsigned long long kd = ~0ull, ke = ~0ull;
     for (int i = team.tr; i < n; i += team.ts) {
         const int8_t a = locA ? sA[i] : ld_cg(pubA + i);
         const int8_t b = locB ? sB[i] : ld_cg(pubB + i);
-        const uint8_t di = a != b;
+        const bool di = a != b;
         d[i] = di;
-        cl += di;
+        cnt += di;
+        if (!REPLAY) {
+            const unsigned long long key = (mix64(r64 + 0x9E3779B97F4A7C15ull * (unsigned long long)(i + 1)) &
+                                            0xFFFFFFFF00000000ull) | (unsigned)i;
+            if (di) kd = min(kd, key);
+            else ke = min(ke, key);
+        }
+        if (D.has_h && locA) hs += (long long)B.h[i] * a;
     }
-    team.sync();
-    long long cnt = team.sum(cl);
+    for (int w = team.tr; w < nwords; w += team.ts) X.vis[w] = 0u;
+    team.reduce(cnt, kd, ke, hs);
     const bool gflip = cnt > (long long)(n / 2);
+    long long dEa = 0, dEb = 0;
     if (gflip) {
         for (int i = team.tr; i < n; i += team.ts) {
             if (locA) { sA[i] = (int8_t)-sA[i]; fA[i] = -fA[i]; }
             d[i] ^= 1;
         }
         cnt = n - cnt;
+        if (team.tr == 0) dEa = -2 * hs;   // E(-s) = E(s) - 2 sum h s
         team.sync();
     }
-    bool moved = false;
+    if (threadIdx.x == 0) P.subtick(PROF_ICM_DIFF);
+    int seed = -1;
     if (REPLAY) {
         const long long idx = (long long)ls * D.nc + q;
         const long long traced = (idx < (long long)A.replay.n_icm) ? A.replay.icm_seed[idx] : -2;
@@ -178,130 +214,202 @@ __device__ void icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOC
                 if (team.tr == 0) dev_fail(A.status, A.abort_flag, DEV_BAD_INDEX, where_err + 1, idx, traced);
                 return;
             }
-            const int seed = A.perm[D.perm_off + traced];
+            seed = A.perm[D.perm_off + traced];
             if (!d[seed]) {
                 if (team.tr == 0) dev_fail(A.status, A.abort_flag, DEV_REPLAY_MISMATCH, where_err + 2, idx, seed);
                 return;
             }
-            if (team.tr == 0) *team.bcast = seed;
         }
     } else if (cnt > 0) {
-        const uint2 key = stream_key(A.seed, STREAM_ICM);
-        const uint4 rnd = philox4x32_10(make_uint4((uint32_t)q, (uint32_t)D.inst_id, (uint32_t)step,
-                                                   (uint32_t)(step >> 32)), key);
-        const int r = (int)bounded32(rnd.x, (uint32_t)cnt);
-        if (team.tr < 32) {
-            const int s = select_rth(d, n, r, team.tr);
-            if (team.tr == 0) *team.bcast = s;
-        }
-    }
-    team.sync();
-    if (cnt > 0) {
-        const int seed = *team.bcast;
+        seed = (int)((gflip ? ke : kd) & 0xFFFFFFFFull);
         if (seed < 0 || seed >= n) {
             if (team.tr == 0) dev_fail(A.status, A.abort_flag, DEV_BAD_INDEX, where_err + 4, q, seed);
             return;
         }
-        for (int i = team.tr; i < n; i += team.ts) parent[i] = i;
-        team.sync();
-        bool ok = true;
-        for (int u = team.tr; u < n; u += team.ts) {
-            if (!d[u]) continue;
-            const int e0 = B.row[u], e1 = B.row[u + 1];
-            for (int a = e0; a < e1; a++) {
-                const int v = (int)(B.adj[a] >> 8);
-                if (v > u && d[v]) ok &= uf_unite(parent, u, v);
-            }
+    }
+    if (threadIdx.x == 0) P.subtick(PROF_ICM_SEED);
+    if (cnt > 0) {
+        // breadth-first growth of the seed's cluster, flipping as it goes
+        if (team.tr == 0) {
+            X.queue[0] = seed;
+            X.vis[seed >> 5] |= 1u << (seed & 31);
+            team.ctl[0] = 0;
+            team.ctl[1] = 1;
         }
-        if (!ok) dev_fail(A.status, A.abort_flag, DEV_UF_LIMIT, where_err + 3, q, 0);
         team.sync();
-        const int root = uf_find(parent, seed);
-        for (int i = team.tr; i < n; i += team.ts) {
-            if (!d[i]) continue;
-            if (uf_find(parent, i) != root) continue;
-            const int e0 = B.row[i], e1 = B.row[i + 1];
-            if (locA) {
-                const int s = sA[i];
-                sA[i] = (int8_t)-s;
-                for (int a = e0; a < e1; a++) {
-                    const uint32_t e = B.adj[a];
-                    atomicAdd(fA + (e >> 8), (int)(int8_t)(e & 0xffu) * (-2 * s));
+        volatile int* vctl = team.ctl;
+        const int lane = threadIdx.x & 31;
+        for (int level = 0; level <= n; level++) {
+            const int lo = vctl[0], hi = vctl[1];
+            team.sync();
+            if (lo == hi) break;
+            for (int base = lo; base < hi; base += team.ts) {
+                const int idx = base + team.tr;
+                const bool have = idx < hi;
+                const int u = have ? X.queue[idx] : 0;
+                int sa = 0, sb = 0, e0 = 0, deg = 0;
+                if (have) {
+                    const int hu = D.has_h ? B.h[u] : 0;
+                    if (locA) { sa = sA[u]; sA[u] = (int8_t)-sa; dEa -= 2 * sa * hu; }
+                    if (locB) { sb = sB[u]; sB[u] = (int8_t)-sb; dEb -= 2 * sb * hu; }
+                    e0 = B.row[u];
+                    deg = B.row[u + 1] - e0;
+                }
+                for (int k = 0; __any_sync(0xffffffffu, k < deg); k++) {
+                    bool found = false;
+                    int v = 0;
+                    if (k < deg) {
+                        const uint32_t e = B.adj[e0 + k];
+                        v = (int)(e >> 8);
+                        const int J = (int)(int8_t)(e & 0xffu);
+                        if (locA) atomicAdd(fA + v, J * (-2 * sa));
+                        if (locB) atomicAdd(fB + v, J * (-2 * sb));
+                        if (d[v]) {
+                            const uint32_t bit = 1u << (v & 31);
+                            found = !(atomicOr(X.vis + (v >> 5), bit) & bit);
+                        } else {
+                            // edge leaving the cluster: s_v is equal in A and B
+                            const int sv = locA ? sA[v] : sB[v];
+                            if (locA) dEa -= 2 * J * sa * sv;
+                            if (locB) dEb -= 2 * J * sb * sv;
+                        }
+                    }
+                    const unsigned m = __ballot_sync(0xffffffffu, found);
+                    if (m) {
+                        const int leader = __ffs(m) - 1;
+                        int slot0 = 0;
+                        if (lane == leader) slot0 = atomicAdd(team.ctl + 1, __popc(m));
+                        slot0 = __shfl_sync(0xffffffffu, slot0, leader);
+                        if (found) X.queue[slot0 + __popc(m & ((1u << lane) - 1u))] = v;
+                    }
                 }
             }
-            if (locB) {
-                const int s = sB[i];
-                sB[i] = (int8_t)-s;
-                for (int a = e0; a < e1; a++) {
-                    const uint32_t e = B.adj[a];
-                    atomicAdd(fB + (e >> 8), (int)(int8_t)(e & 0xffu) * (-2 * s));
-                }
-            }
+            team.sync();
+            if (team.tr == 0) vctl[0] = hi;
+            team.sync();
         }
-        moved = true;
-        team.sync();
+        if (threadIdx.x == 0) P.subtick(PROF_ICM_UNION);
     }
-    // energies of the members held here: E = sum h s + 1/2 sum s f
-    if (locA && (moved || gflip)) {
-        long long v = 0;
-        for (int i = team.tr; i < n; i += team.ts) v += (long long)sA[i] * (2 * (D.has_h ? B.h[i] : 0) + fA[i]);
-        v = team.sum(v);
-        if (team.tr == 0) B.E[rA] = v / 2;
-    }
-    if (locB && moved) {
-        long long v = 0;
-        for (int i = team.tr; i < n; i += team.ts) v += (long long)sB[i] * (2 * (D.has_h ? B.h[i] : 0) + fB[i]);
-        v = team.sum(v);
-        if (team.tr == 0) B.E[rB] = v / 2;
+    if (gflip || cnt > 0) {
+        team.sum2(dEa, dEb);
+        if (team.tr == 0) {
+            if (locA) B.E[rA] += dEa;
+            if (locB && cnt > 0) B.E[rB] += dEb;
+        }
     }
     team.sync();
+    if (threadIdx.x == 0) P.subtick(PROF_ICM_FLIP);
 }
-
 
 // --------------------------------------------------------------- sweeps
 // Colour-class Metropolis sweep of the block's replicas (production).
 // dE_i = -2 s_i (h_i + f_i); accepted with probability min(1, exp(-beta dE))
 // (src/replica.cc:31-38); an accepted flip pushes J_ij * (-2 s_i) into each
-// neighbour's field (the integer form of src/problem.cc:164-181).
+// neighbour's field (the integer form of src/problem.cc:164-181).  With one
+// replica per block (ONE) every thread keeps its energy change and flip
+// count in registers until a phase boundary; with several, warps aggregate
+// per replica before touching shared memory.
+template <bool ONE>
 __device__ void colored_sweep(const EngineArgs& A, const BlockCtx& B, unsigned long long sweep_idx,
                               int32_t* s_col, const uint32_t* s_thr, int* s_dEp, unsigned* s_flp,
                               unsigned long long* s_flips, long long* s_bestE, int* s_improved,
                               int* s_misc, bool best_per_phase) {
     const InstanceDesc& D = B.D;
-    const int T = blockDim.x, tid = threadIdx.x;
-    const int npad = D.n_pad, rpc = D.rpc;
-    ThreadRng rng;
+    const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31;
+    const int npad = D.n_pad, rpc = ONE ? 1 : D.rpc;
+    const int32_t* row = B.row;
+    const uint32_t* adj = B.adj;
+    const int kmax = D.kmax;
+    ThreadRng12 rng;
     rng.start(stream_key(A.seed, STREAM_SWEEP), blockIdx.x * blockDim.x + tid, sweep_idx);
+    int acc_de = 0;
+    unsigned acc_fl = 0;
     for (int c = 0; c < D.ncolors; c++) {
         const int c0 = s_col[c];
         const int Sc = s_col[c + 1] - c0;
-        const int items = rpc * Sc;
-        for (int it = tid; it < items; it += T) {
-            const int j = it / Sc;
-            const int i = c0 + (it - j * Sc);
-            int8_t* sp = B.spin + j * npad;
-            int32_t* fd = B.field + j * npad;
-            const int s = sp[i];
-            const int f = fd[i] + (D.has_h ? B.h[i] : 0);
-            const int de = -2 * s * f;
-            bool acc = de <= 0;
-            if (!acc) {
-                const uint32_t thr = s_thr[B.tb[j] + min(de >> 1, D.kmax)];
-                acc = (rng.next() < thr) || (thr == 0xFFFFFFFFu);
+        if (ONE) {
+            int8_t* sp = B.spin;
+            int32_t* fd = B.field;
+            const uint32_t* thr_row = s_thr + B.tb[0];
+            for (int i = c0 + tid; i < c0 + Sc; i += T) {
+                const int s = sp[i];
+                const int f = fd[i] + (D.has_h ? B.h[i] : 0);
+                const int de = -2 * s * f;
+                bool acc = de <= 0;
+                if (!acc) {
+                    const uint32_t thr = thr_row[min(de >> 1, kmax)];
+                    acc = (rng.next() < thr) || (thr == 0xFFFFFFFFu);
+                }
+                if (acc) {
+                    sp[i] = (int8_t)-s;
+                    acc_de += de;
+                    acc_fl++;
+                    const int dl = -2 * s;
+                    const int e1 = row[i + 1];
+                    for (int a = row[i]; a < e1; a++) {
+                        const uint32_t e = adj[a];
+                        atomicAdd(fd + (e >> 8), (int)(int8_t)(e & 0xffu) * dl);
+                    }
+                }
             }
-            if (acc) {
-                sp[i] = (int8_t)-s;
-                atomicAdd(s_dEp + j, de);
-                atomicAdd(s_flp + j, 1u);
-                const int dl = -2 * s;
-                const int e0 = B.row[i], e1 = B.row[i + 1];
-                for (int a = e0; a < e1; a++) {
-                    const uint32_t e = B.adj[a];
-                    atomicAdd(fd + (e >> 8), (int)(int8_t)(e & 0xffu) * dl);
+        } else {
+            const int items = rpc * Sc;
+            const int items_w = (items + 31) & ~31;   // whole warps iterate together
+            for (int it = tid; it < items_w; it += T) {
+                int j = -1, de = 0;
+                bool acc = false;
+                if (it < items) {
+                    j = it / Sc;
+                    const int i = c0 + (it - j * Sc);
+                    int8_t* sp = B.spin + j * npad;
+                    int32_t* fd = B.field + j * npad;
+                    const int s = sp[i];
+                    const int f = fd[i] + (D.has_h ? B.h[i] : 0);
+                    de = -2 * s * f;
+                    acc = de <= 0;
+                    if (!acc) {
+                        const uint32_t thr = s_thr[B.tb[j] + min(de >> 1, kmax)];
+                        acc = (rng.next() < thr) || (thr == 0xFFFFFFFFu);
+                    }
+                    if (acc) {
+                        sp[i] = (int8_t)-s;
+                        const int dl = -2 * s;
+                        const int e1 = row[i + 1];
+                        for (int a = row[i]; a < e1; a++) {
+                            const uint32_t e = adj[a];
+                            atomicAdd(fd + (e >> 8), (int)(int8_t)(e & 0xffu) * dl);
+                        }
+                    }
+                }
+                // one shared-memory update per replica per warp instead of per flip
+                const int key = acc ? j : -1;
+                const unsigned grp = __match_any_sync(0xffffffffu, key);
+                if (acc) {
+                    const int sde = __reduce_add_sync(grp, de);
+                    if (lane == __ffs(grp) - 1) {
+                        atomicAdd(s_dEp + j, sde);
+                        atomicAdd(s_flp + j, (unsigned)__popc(grp));
+                    }
                 }
             }
         }
+        const bool track = best_per_phase || c + 1 == D.ncolors;
+        if (ONE && track) {
+            int v = acc_de;
+            unsigned f = acc_fl;
+            for (int o = 16; o > 0; o >>= 1) {
+                v += __shfl_xor_sync(0xffffffffu, v, o);
+                f += __shfl_xor_sync(0xffffffffu, f, o);
+            }
+            if (lane == 0 && (v != 0 || f != 0)) {
+                atomicAdd(s_dEp, v);
+                atomicAdd(s_flp, f);
+            }
+            acc_de = 0;
+            acc_fl = 0;
+        }
         __syncthreads();
-        if (!best_per_phase && c + 1 < D.ncolors) continue;
+        if (!track) continue;
         // phase boundary: fold the phase's energy change, track the best state
         for (int jj = tid; jj < rpc; jj += T) {
             const int r = B.r0 + jj;
@@ -321,7 +429,7 @@ __device__ void colored_sweep(const EngineArgs& A, const BlockCtx& B, unsigned l
         __syncthreads();
         if (s_misc[1] > 0) {
             for (int idx = tid; idx < rpc * npad; idx += T) {
-                const int j = idx / npad;
+                const int j = ONE ? 0 : idx / npad;
                 if (s_improved[j]) A.best_state[D.spin_off + (long long)B.r0 * npad + idx] = B.spin[idx];
             }
             __syncthreads();
@@ -413,7 +521,8 @@ __device__ void replay_sweep(const EngineArgs& A, const BlockCtx& B, int ls, int
 __device__ void exchange_reference_order(const EngineArgs& A, const BlockCtx& B, unsigned long long step,
                                          uint32_t* s_order, const double* s_dbeta, unsigned* s_att,
                                          unsigned* s_succ, float* s_xlogu, uint32_t* s_xrand,
-                                         int* s_lvl, uint32_t* s_tmp, int* s_misc) {
+                                         int* s_lvl, uint32_t* s_tmp, int* s_misc, Prof& P) {
+    if (threadIdx.x == 0) P.subtick(PROF_X_SHUFFLE);
     const InstanceDesc& D = B.D;
     const int tid = threadIdx.x, T = blockDim.x;
     const int nt = D.nt, C = D.chains, m = nt - 1;
@@ -434,72 +543,80 @@ __device__ void exchange_reference_order(const EngineArgs& A, const BlockCtx& B,
         }
     }
     __syncthreads();
-    for (int round = 0; round < C; round++) {
-        // level of attempt i = 1 + max level of earlier attempts on pairs
-        // order[i]-1 and order[i]+1 of the same chain
-        for (int i = tid; i < m; i += T) {
-            s_lvl[i] = 1;
-            s_tmp[s_order[i]] = (uint32_t)i;   // position of each pair in this pass
-        }
-        __syncthreads();
-        for (;;) {
-            int changed = 0;
-            for (int i = tid; i < m; i += T) {
-                const int kb = (int)s_order[i];
-                const int c = (round * m + i) % C;
-                int lv = 1;
-                if (kb > 0) {
-                    const int jn = (int)s_tmp[kb - 1];
-                    if (jn < i && (round * m + jn) % C == c) lv = max(lv, ((volatile int*)s_lvl)[jn] + 1);
-                }
-                if (kb + 1 < m) {
-                    const int jn = (int)s_tmp[kb + 1];
-                    if (jn < i && (round * m + jn) % C == c) lv = max(lv, ((volatile int*)s_lvl)[jn] + 1);
-                }
-                if (lv != s_lvl[i]) { s_lvl[i] = lv; changed = 1; }
+    if (threadIdx.x == 0) P.subtick(PROF_X_DRAW);
+    // one warp walks the rounds; the rest of the block waits at the end
+    if (tid < 32) {
+        const int lane = tid;
+        for (int round = 0; round < C; round++) {
+            // level of attempt i = 1 + max level of earlier attempts on the
+            // neighbouring pairs of the same chain
+            for (int i = lane; i < m; i += 32) {
+                s_lvl[i] = 1;
+                s_tmp[s_order[i]] = (uint32_t)i;   // position of each pair in this pass
             }
-            if (!__syncthreads_or(changed)) break;
-        }
-        int maxl = 0;
-        for (int i = tid; i < m; i += T) maxl = max(maxl, s_lvl[i]);
-        if (tid == 0) s_misc[2] = 0;
-        __syncthreads();
-        if (maxl) atomicMax(s_misc + 2, maxl);
-        __syncthreads();
-        const int L = s_misc[2];
-        for (int lv = 1; lv <= L; lv++) {
-            for (int i = tid; i < m; i += T) {
-                if (s_lvl[i] != lv) continue;
-                const int kb = (int)s_order[i];
-                const int a = round * m + i;
-                const int c = a % C;
-                const int k = c * nt + kb;
-                const uint32_t r1 = B.slot[k], r2 = B.slot[k + 1];
-                const double x = s_dbeta[kb] * (double)(B.E[r1] - B.E[r2]);
-                s_att[k]++;
-                if (x > 0.0 || (double)s_xlogu[a] < x) {
-                    s_succ[k]++;
-                    B.slot[k] = r2;
-                    B.slot[k + 1] = r1;
+            __syncwarp();
+            for (int iter = 0; iter <= m; iter++) {
+                int changed = 0;
+                for (int i = lane; i < m; i += 32) {
+                    const int kb = (int)s_order[i];
+                    const int c = (round * m + i) % C;
+                    int lv = 1;
+                    if (kb > 0) {
+                        const int jn = (int)s_tmp[kb - 1];
+                        if (jn < i && (round * m + jn) % C == c) lv = max(lv, ((volatile int*)s_lvl)[jn] + 1);
+                    }
+                    if (kb + 1 < m) {
+                        const int jn = (int)s_tmp[kb + 1];
+                        if (jn < i && (round * m + jn) % C == c) lv = max(lv, ((volatile int*)s_lvl)[jn] + 1);
+                    }
+                    if (lv != s_lvl[i]) { s_lvl[i] = lv; changed = 1; }
                 }
+                const bool again = __any_sync(0xffffffffu, changed);
+                __syncwarp();
+                if (!again) break;
             }
-            __syncthreads();
-        }
-        // reshuffle: rank the pairs by fresh random keys (ties by position)
-        const uint32_t* keys = s_xrand + round * m;
-        for (int i = tid; i < m; i += T) {
-            const uint32_t ki = keys[i];
-            int rank = 0;
-            for (int j = 0; j < m; j++) {
-                const uint32_t kj = keys[j];
-                rank += (kj < ki) || (kj == ki && j < i);
+            int maxl = 0;
+            for (int i = lane; i < m; i += 32) maxl = max(maxl, s_lvl[i]);
+            const int L = __reduce_max_sync(0xffffffffu, maxl);
+            if (lane == 0) P.subtick(PROF_X_LEVELS);
+            for (int lv = 1; lv <= L; lv++) {
+                for (int i = lane; i < m; i += 32) {
+                    if (s_lvl[i] != lv) continue;
+                    const int kb = (int)s_order[i];
+                    const int a = round * m + i;
+                    const int c = a % C;
+                    const int k = c * nt + kb;
+                    const uint32_t r1 = B.slot[k], r2 = B.slot[k + 1];
+                    const double x = s_dbeta[kb] * (double)(B.E[r1] - B.E[r2]);
+                    s_att[k]++;
+                    if (x > 0.0 || (double)s_xlogu[a] < x) {
+                        s_succ[k]++;
+                        B.slot[k] = r2;
+                        B.slot[k + 1] = r1;
+                    }
+                }
+                __syncwarp();
             }
-            s_tmp[rank] = s_order[i];
+            if (lane == 0) P.subtick(PROF_X_APPLY);
+            // reshuffle: rank the pairs by fresh random keys (ties by position)
+            const uint32_t* keys = s_xrand + round * m;
+            for (int i = lane; i < m; i += 32) {
+                const uint32_t ki = keys[i];
+                int rank = 0;
+                for (int j = 0; j < m; j++) {
+                    const uint32_t kj = keys[j];
+                    rank += (kj < ki) || (kj == ki && j < i);
+                }
+                s_tmp[rank] = s_order[i];
+            }
+            __syncwarp();
+            for (int i = lane; i < m; i += 32) s_order[i] = s_tmp[i];
+            __syncwarp();
+            if (lane == 0) P.subtick(PROF_X_SHUFFLE);
         }
-        __syncthreads();
-        for (int i = tid; i < m; i += T) s_order[i] = s_tmp[i];
-        __syncthreads();
     }
+    __syncthreads();
+    (void)s_misc;
 }
 
 // Deterministic even/odd exchange: per chain, all even pairs, then all odd
@@ -568,7 +685,7 @@ __device__ void exchange_replay(const EngineArgs& A, const BlockCtx& B, int ls, 
 
 // ---------------------------------------------------------------- kernel
 template <bool REPLAY, bool BLOCKTEAM>
-__global__ void __launch_bounds__(1024) pt_engine_kernel(const EngineArgs A) {
+__global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) {
     extern __shared__ __align__(128) uint8_t smem[];
     const SmemPlan& S = A.sm;
     const int tid = threadIdx.x, T = blockDim.x;
@@ -609,7 +726,7 @@ __global__ void __launch_bounds__(1024) pt_engine_kernel(const EngineArgs A) {
     uint8_t* s_icm = smem + S.icm;
     int* s_misc = sm_ptr<int>(smem, S.misc);
     long long* s_team_acc = sm_ptr<long long>(smem, S.misc + 64);
-    int* s_team_bc = sm_ptr<int>(smem, S.misc + 64 + 8 * 32);
+    int* s_team_bc = sm_ptr<int>(smem, S.misc + 64 + 8 * 32);   // 2 ints per team
 
     const int32_t* g_row = A.row + D.row_off;
     const uint32_t* g_adj = A.adj + D.adj_off;
@@ -681,6 +798,9 @@ __global__ void __launch_bounds__(1024) pt_engine_kernel(const EngineArgs A) {
     __syncthreads();
 
     const bool icm_on = (A.phase_mask & PHASE_ICM) && D.nc > 0 && D.chains >= 2;
+    Prof P;
+    P.init((A.prof != nullptr) && tid == 0);
+    const long long t_start = P.mark;
     const bool best_pp = (A.flags & ENGINE_BEST_PER_PHASE) != 0;
     for (int ls = 0; ls < A.nsteps; ls++) {
         if (tid == 0) s_misc[3] = *abortf;
@@ -695,11 +815,12 @@ __global__ void __launch_bounds__(1024) pt_engine_kernel(const EngineArgs A) {
                     replay_sweep(A, B, ls, sw, sweep_idx, s_ptab, s_flips, s_bestE);
                     __syncthreads();
                 } else {
-                    colored_sweep(A, B, sweep_idx, s_col, s_thr, s_dEp, s_flp, s_flips, s_bestE, s_improved,
-                                  s_misc, best_pp);
+                    colored_sweep<BLOCKTEAM>(A, B, sweep_idx, s_col, s_thr, s_dEp, s_flp, s_flips, s_bestE,
+                                             s_improved, s_misc, best_pp);
                 }
             }
         }
+        P.tick(PROF_SWEEP);
         if (D.group > 1) {
             // publish this block's energies (and spins, for ICM partners)
             for (int j = tid; j < rpc; j += T) A.energy_pub[parity * A.energy_pub_half + D.rep_off + B.r0 + j] = B.E[B.r0 + j];
@@ -712,10 +833,11 @@ __global__ void __launch_bounds__(1024) pt_engine_kernel(const EngineArgs A) {
                 if (r < B.r0 || r >= B.r0 + rpc) B.E[r] = ld_cg(A.energy_pub + parity * A.energy_pub_half + D.rep_off + r);
             __syncthreads();
         }
+        P.tick(PROF_BARRIER);
         if (A.phase_mask & PHASE_EXCHANGE) {
             if (REPLAY) exchange_replay(A, B, ls, s_beta, s_att, s_succ);
             else if (A.flags & ENGINE_EXCHANGE_EVEN_ODD) exchange_even_odd(A, B, step, s_dbeta, s_att, s_succ);
-            else exchange_reference_order(A, B, step, s_order, s_dbeta, s_att, s_succ, s_xlogu, s_xrand, s_lvl, s_tmp, s_misc);
+            else exchange_reference_order(A, B, step, s_order, s_dbeta, s_att, s_succ, s_xlogu, s_xrand, s_lvl, s_tmp, s_misc, P);
             for (int s = tid; s < R; s += T) {
                 const uint32_t r = B.slot[s];
                 if ((int)r >= B.r0 && (int)r < B.r0 + rpc) {
@@ -725,27 +847,26 @@ __global__ void __launch_bounds__(1024) pt_engine_kernel(const EngineArgs A) {
             }
             __syncthreads();
         }
+        P.tick(PROF_EXCHANGE);
         if (icm_on) {
             // pairs q = cp*nc + kk: slots (2cp)*nt + k and (2cp+1)*nt + k, k = nt-1-kk
             const int npairs = D.nc * (D.chains / 2);
             if (BLOCKTEAM) {
                 Team<true> team{tid, T, s_team_acc, s_team_bc};
-                int* parent = reinterpret_cast<int*>(s_icm);
-                uint8_t* d = s_icm + (size_t)S.max_n_pad * 4;
+                const IcmScratch X = icm_scratch(s_icm, S.max_n_pad);
                 for (int q = 0; q < npairs; q++) {
                     const int cp = q / D.nc, kk = q - cp * D.nc, k = nt - 1 - kk;
                     const int rA = (int)B.slot[(2 * cp) * nt + k], rB = (int)B.slot[(2 * cp + 1) * nt + k];
                     const bool mine = (rA >= B.r0 && rA < B.r0 + rpc) || (rB >= B.r0 && rB < B.r0 + rpc);
                     if (!mine) continue;
-                    icm_pair<true, REPLAY>(A, B, team, q, rA, rB, step, ls, parent, d, 30);
+                    icm_pair<true, REPLAY>(A, B, team, q, rA, rB, step, ls, X, 30, P);
                 }
             } else {
                 const int warp = tid >> 5, lane = tid & 31;
                 const int teams = min(S.teams, T >> 5);
                 if (warp < teams) {
-                    Team<false> team{lane, 32, s_team_acc + warp, s_team_bc + warp};
-                    int* parent = reinterpret_cast<int*>(s_icm + (size_t)warp * S.icm_team_bytes);
-                    uint8_t* d = s_icm + (size_t)warp * S.icm_team_bytes + (size_t)S.max_n_pad * 4;
+                    Team<false> team{lane, 32, s_team_acc + warp, s_team_bc + 2 * warp};
+                    const IcmScratch X = icm_scratch(s_icm + (size_t)warp * S.icm_team_bytes, S.max_n_pad);
                     int e = 0;
                     for (int q = 0; q < npairs; q++) {
                         const int cp = q / D.nc, kk = q - cp * D.nc, k = nt - 1 - kk;
@@ -753,14 +874,19 @@ __global__ void __launch_bounds__(1024) pt_engine_kernel(const EngineArgs A) {
                         const bool mine = (rA >= B.r0 && rA < B.r0 + rpc) || (rB >= B.r0 && rB < B.r0 + rpc);
                         if (!mine) continue;
                         if ((e++ % teams) != warp) continue;
-                        icm_pair<false, REPLAY>(A, B, team, q, rA, rB, step, ls, parent, d, 30);
+                        icm_pair<false, REPLAY>(A, B, team, q, rA, rB, step, ls, X, 30, P);
                     }
                 }
             }
             __syncthreads();
         }
+        P.tick(PROF_ICM);
     }
     __syncthreads();
+    if (P.on) {
+        P.c[PROF_TOTAL] = clock64() - t_start;
+        for (int q = 0; q < PROF_PHASES; q++) A.prof[(size_t)blockIdx.x * PROF_PHASES + q] += (unsigned long long)P.c[q];
+    }
     // ---- write the block's state back
     {
         const long long base = D.spin_off + (long long)B.r0 * npad;

@@ -15,7 +15,7 @@ enum DevErr : int {
     DEV_OK = 0,
     DEV_BARRIER_TIMEOUT = 1,   // a group barrier waited longer than its limit
     DEV_TMA_TIMEOUT = 2,       // a bulk-copy mbarrier never completed
-    DEV_UF_LIMIT = 3,          // union-find retry cap exceeded
+    DEV_UF_LIMIT = 3,          // cluster labelling did not converge within its round cap
     DEV_REPLAY_MISMATCH = 4,   // a replay trace disagrees with the device state
     DEV_BAD_INDEX = 5,         // an index failed a bounds check
     DEV_ABORTED = 6,           // another block aborted first
@@ -94,6 +94,63 @@ struct ThreadRng {
         buf.x = buf.y;
         buf.y = buf.z;
         buf.z = buf.w;
+        avail--;
+        return r;
+    }
+};
+
+// Three Philox blocks with interleaved rounds (independent chains overlap).
+__device__ __forceinline__ void philox4x32_10_x3(uint4& a, uint4& b, uint4& c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        const uint32_t alo0 = 0xD2511F53u * a.x, ahi0 = __umulhi(0xD2511F53u, a.x);
+        const uint32_t alo1 = 0xCD9E8D57u * a.z, ahi1 = __umulhi(0xCD9E8D57u, a.z);
+        const uint32_t blo0 = 0xD2511F53u * b.x, bhi0 = __umulhi(0xD2511F53u, b.x);
+        const uint32_t blo1 = 0xCD9E8D57u * b.z, bhi1 = __umulhi(0xCD9E8D57u, b.z);
+        const uint32_t clo0 = 0xD2511F53u * c.x, chi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t clo1 = 0xCD9E8D57u * c.z, chi1 = __umulhi(0xCD9E8D57u, c.z);
+        a = make_uint4(ahi1 ^ a.y ^ k.x, alo1, ahi0 ^ a.w ^ k.y, alo0);
+        b = make_uint4(bhi1 ^ b.y ^ k.x, blo1, bhi0 ^ b.w ^ k.y, blo0);
+        c = make_uint4(chi1 ^ c.y ^ k.x, clo1, chi0 ^ c.w ^ k.y, clo0);
+        k.x += 0x9E3779B9u;
+        k.y += 0xBB67AE85u;
+    }
+}
+
+// A per-thread Philox stream buffered twelve words at a time; the sweep
+// fills it before its first colour class so that no draw waits on a Philox
+// chain inside a class.
+struct ThreadRng12 {
+    uint4 b0, b1, b2;
+    uint32_t avail;
+    uint32_t calls;
+    uint4 ctr;   // (thread id, sweep lo, sweep hi, block index)
+    uint2 key;
+
+    __device__ __forceinline__ void start(uint2 k, uint32_t tid, unsigned long long sweep) {
+        key = k;
+        ctr = make_uint4(tid, (uint32_t)sweep, (uint32_t)(sweep >> 32), 0u);
+        calls = 0;
+        refill();
+    }
+    __device__ __forceinline__ void refill() {
+        uint4 a = ctr, b = ctr, c = ctr;
+        a.w = calls;
+        b.w = calls + 1;
+        c.w = calls + 2;
+        calls += 3;
+        philox4x32_10_x3(a, b, c, key);
+        b0 = a;
+        b1 = b;
+        b2 = c;
+        avail = 12;
+    }
+    __device__ __forceinline__ uint32_t next() {
+        if (avail == 0) refill();
+        const uint32_t r = b0.x;
+        b0 = make_uint4(b0.y, b0.z, b0.w, b1.x);
+        b1 = make_uint4(b1.y, b1.z, b1.w, b2.x);
+        b2 = make_uint4(b2.y, b2.z, b2.w, 0u);
         avail--;
         return r;
     }

@@ -117,6 +117,7 @@ struct EngineArgs {
     int32_t phase_mask;           // 1 sweep, 2 exchange, 4 ICM
     int32_t flags;                // ENGINE_* flags
     unsigned long long seed;
+    unsigned long long* prof;     // optional: per block, clock64 cycles per phase (PROF_PHASES)
     SmemPlan sm;
     ReplayArgs replay;
 };
@@ -128,5 +129,17 @@ enum EngineFlags : int32_t {
 };
 
 enum PhaseBits : int32_t { PHASE_SWEEP = 1, PHASE_EXCHANGE = 2, PHASE_ICM = 4 };
+
+// Phase timers: cycles spent per block in sweep, publish+barrier, exchange
+// and ICM, plus the whole launch.
+// Slots 5.. split ICM (overlap+count, seed choice, union, flip, energies) and
+// the exchange (draws, dependency levels, attempts, reshuffle) as seen by
+// thread 0 of the block.
+enum ProfSlots : int32_t {
+    PROF_SWEEP = 0, PROF_BARRIER = 1, PROF_EXCHANGE = 2, PROF_ICM = 3, PROF_TOTAL = 4,
+    PROF_ICM_DIFF = 5, PROF_ICM_SEED = 6, PROF_ICM_UNION = 7, PROF_ICM_FLIP = 8, PROF_ICM_ENERGY = 9,
+    PROF_X_DRAW = 10, PROF_X_LEVELS = 11, PROF_X_APPLY = 12, PROF_X_SHUFFLE = 13,
+    PROF_PHASES = 14
+};
 
 }  // namespace pticm

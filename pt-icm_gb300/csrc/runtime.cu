@@ -133,7 +133,8 @@ struct pticm_ctx {
     DArr<int8_t> d_spins, d_pub, d_best_state;
     DArr<int32_t> d_fields;
     DArr<long long> d_E, d_Epub, d_bestE;
-    DArr<unsigned long long> d_flips, d_bestSweep, d_att, d_succ, d_mismatch;
+    DArr<unsigned long long> d_flips, d_bestSweep, d_att, d_succ, d_mismatch, d_prof;
+    bool profiling = false;
     DArr<unsigned int> d_bar;
     DArr<int> d_abort;
     DArr<DevStatus> d_status;
@@ -186,10 +187,11 @@ SmemPlan make_plan(const InstanceDesc& D, bool replay, int teams, int threads, b
     S.xrand = take((uint64_t)D.chains * m * 4 + 16);
     S.xlevel = take((uint64_t)D.nt * 4);
     S.xpos = take((uint64_t)D.nt * 4);
-    S.icm_team_bytes = align16((uint64_t)D.n_pad * 4 + D.n_pad);
+    // BFS queue (4 B/site), overlap flags (1 B/site), visited bits (n_pad is a multiple of 16)
+    S.icm_team_bytes = align16((uint64_t)D.n_pad * 5 + 4 * ((uint64_t)(D.n_pad + 31) / 32));
     S.teams = teams;
     S.icm = take((uint64_t)teams * S.icm_team_bytes);
-    S.misc = take(512);
+    S.misc = take(64 + 8 * 32 + 4 * 64 + 64);
     S.total = (uint32_t)off;
     S.max_n_pad = D.n_pad;
     S.max_kmax = D.kmax;
@@ -301,6 +303,7 @@ EngineArgs make_args(pticm_ctx* c) {
     A.sweeps = (int)c->o.sweeps;
     A.seed = c->o.seed;
     A.sm = c->plan;
+    A.prof = (c->profiling && c->d_prof.n >= (size_t)c->group * PROF_PHASES) ? c->d_prof.p : nullptr;
     A.flags = (c->o.best_per_phase ? ENGINE_BEST_PER_PHASE : 0) | (c->o.exchange == 1 ? ENGINE_EXCHANGE_EVEN_ODD : 0);
     return A;
 }
@@ -310,7 +313,7 @@ int read_status(pticm_ctx* c, const char* what) {
     CK(cudaMemcpy(&st, c->d_status.p, sizeof(st), cudaMemcpyDeviceToHost));
     if (st.error) {
         static const char* names[] = {"ok", "group barrier wait expired", "bulk-copy wait expired",
-                                      "union-find retry cap", "replay trace mismatch", "index out of range",
+                                      "cluster labelling round cap", "replay trace mismatch", "index out of range",
                                       "aborted"};
         const char* nm = (st.error >= 0 && st.error <= 6) ? names[st.error] : "unknown";
         return fail(PTICM_ERR_DEVICE, std::string(what) + ": device reported " + nm + " at site " +
@@ -774,6 +777,38 @@ int pticm_verify(pticm_ctx* c, uint64_t* mismatches) {
     CK(cudaMemcpyAsync(&mm, c->d_mismatch.p, sizeof(mm), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     *mismatches = mm;
+    return PTICM_OK;
+}
+
+int pticm_set_profiling(pticm_ctx* c, int enable) {
+    if (!c) return fail(PTICM_ERR_INVALID, "null argument");
+    c->profiling = enable != 0;
+    if (c->profiling) CK(c->d_prof.alloc((size_t)std::max(c->R, 1) * PROF_PHASES));
+    return PTICM_OK;
+}
+
+int pticm_get_profile(pticm_ctx* c, double* mean_ms, double* max_ms) {
+    static_assert(PROF_PHASES == 14, "profile slots");
+    if (!c) return fail(PTICM_ERR_INVALID, "null argument");
+    if (!c->profiling) return fail(PTICM_ERR_INVALID, "profiling is not enabled");
+    CK(cudaStreamSynchronize(c->stream));
+    std::vector<unsigned long long> v;
+    CK(c->d_prof.download(v));
+    int dev = 0, khz = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, dev));
+    const double to_ms = 1.0 / (double)std::max(khz, 1);
+    const int blocks = std::max(c->group, 1);
+    for (int q = 0; q < PROF_PHASES; q++) {
+        double sum = 0, mx = 0;
+        for (int b = 0; b < blocks; b++) {
+            const double x = (double)v[(size_t)b * PROF_PHASES + q] * to_ms;
+            sum += x;
+            mx = std::max(mx, x);
+        }
+        if (mean_ms) mean_ms[q] = sum / blocks;
+        if (max_ms) max_ms[q] = mx;
+    }
     return PTICM_OK;
 }
 

@@ -85,6 +85,8 @@ def lib():
         "pticm_verify": [P, P],
         "pticm_replay": [P, C.POINTER(Trace)],
         "pticm_philox_probe": [P, P, P, C.c_int],
+        "pticm_set_profiling": [P, C.c_int],
+        "pticm_get_profile": [P, P, P],
     }
     for name, args in sigs.items():
         f = getattr(L, name)
@@ -242,6 +244,18 @@ class Context:
         nc = C.c_uint32()
         _check(lib().pticm_get_ladder(self._h, _p(b), _p(s2r), C.byref(nc)))
         return b, s2r, nc.value
+
+    def set_profiling(self, enable=True):
+        _check(lib().pticm_set_profiling(self._h, int(enable)))
+
+    def profile(self):
+        """Mean and max over blocks of ms in (sweep, barrier, exchange, ICM, total)."""
+        mean = np.zeros(14)
+        mx = np.zeros(14)
+        _check(lib().pticm_get_profile(self._h, _p(mean), _p(mx)))
+        names = ("sweep", "barrier", "exchange", "icm", "total", "icm_diff", "icm_seed", "icm_union",
+                 "icm_flip", "icm_energy", "x_draw", "x_levels", "x_apply", "x_shuffle")
+        return dict(zip(names, mean)), dict(zip(names, mx))
 
     def verify(self) -> int:
         mm = C.c_uint64()

@@ -89,10 +89,14 @@ typedef struct pticm_opts {
     uint32_t chains;        /* replicas per temperature (2 in the reference)  */
     uint32_t sweeps;        /* --sweeps per PT step                           */
     uint32_t icm;           /* --icm                                          */
-    uint32_t exchange;      /* 0 reference attempt order, 1 even/odd rounds   */
-    uint32_t best_per_phase;/* 1: best state checked after every colour class */
+    uint32_t exchange;      /* 1 even/odd rounds (default), 0 the reference's */
+                            /* shuffled attempt order (src/replica_exchange.cc)*/
+    uint32_t best_per_phase;/* 1: best state checked after every colour class,*/
+                            /* 0 (default): after every sweep                 */
     uint32_t block_threads; /* 0 = automatic                                  */
     uint32_t replicas_per_block; /* 0 = automatic                             */
+    uint32_t icm_algo;      /* cluster search: 0 auto, 1 breadth-first,       */
+                            /* 2 union-find, 3 label propagation              */
 } pticm_opts;
 
 void pticm_opts_default(pticm_opts* o);

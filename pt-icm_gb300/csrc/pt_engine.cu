@@ -52,6 +52,35 @@ struct Prof {
     }
 };
 
+// ------------------------------------------------------------ union-find
+// Concurrent union-find in shared memory: roots are hooked larger-under-
+// smaller with CAS (parent indices strictly decrease, so no cycle forms) and
+// finds halve paths.  Loops are capped; -1 / false report the cap.
+__device__ __forceinline__ int uf_find(volatile int* parent, int x) {
+    for (int it = 0; it < (1 << 20); it++) {
+        const int p = parent[x];
+        if (p == x) return x;
+        const int gp = parent[p];
+        if (gp == p) return p;
+        parent[x] = gp;
+        x = gp;
+    }
+    return -1;
+}
+
+__device__ __forceinline__ bool uf_unite(int* parent, int a, int b) {
+    volatile int* vp = parent;
+    for (int it = 0; it < (1 << 20); it++) {
+        a = uf_find(vp, a);
+        b = uf_find(vp, b);
+        if (a < 0 || b < 0) return false;
+        if (a == b) return true;
+        if (a < b) { const int t = a; a = b; b = t; }
+        if (atomicCAS(parent + a, a, b) == a) return true;
+    }
+    return false;
+}
+
 // ---------------------------------------------------------- team helpers
 // An ICM "team" is either one warp (many pairs per block) or the whole block
 // (one pair per block).  Block-wide reductions go through shared scratch.
@@ -228,7 +257,92 @@ __device__ void icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOC
         }
     }
     if (threadIdx.x == 0) P.subtick(PROF_ICM_SEED);
-    if (cnt > 0) {
+    const int algo = A.flags & ENGINE_ICM_MASK;
+    if (cnt > 0 && algo != ENGINE_ICM_BFS) {
+        // label the components of the whole overlap subgraph, then flip the
+        // sites sharing the seed's label
+        int* lab = X.queue;
+        volatile int* vl = lab;
+        bool ok = true;
+        for (int i = team.tr; i < n; i += team.ts) lab[i] = d[i] ? i : n;
+        team.sync();
+        if (algo == ENGINE_ICM_UNION_FIND) {
+            for (int u = team.tr; u < n; u += team.ts) {
+                if (!d[u]) continue;
+                const int e1 = B.row[u + 1];
+                for (int a = B.row[u]; a < e1; a++) {
+                    const int v = (int)(B.adj[a] >> 8);
+                    if (v > u && d[v]) ok &= uf_unite(lab, u, v);
+                }
+            }
+            team.sync();
+        } else {
+            // minimum-label propagation with root hooking and pointer jumping
+            // (Shiloach-Vishkin style); labels only decrease and always name
+            // a site of the same component
+            bool conv = false;
+            for (int round = 0; round < 512 && !conv; round++) {
+                int changed = 0;
+                for (int u = team.tr; u < n; u += team.ts) {
+                    if (!d[u]) continue;
+                    const int lu = vl[u];
+                    int best = lu;
+                    const int e1 = B.row[u + 1];
+                    for (int a = B.row[u]; a < e1; a++) {
+                        const int v = (int)(B.adj[a] >> 8);
+                        if (d[v]) best = min(best, vl[v]);
+                    }
+                    if (best < lu) {
+                        atomicMin(lab + lu, best);
+                        atomicMin(lab + u, best);
+                        changed = 1;
+                    }
+                }
+                conv = !(BLOCK ? (__syncthreads_or(changed) != 0) : (__any_sync(0xffffffffu, changed) != 0));
+                if (!BLOCK) __syncwarp();
+                for (int u = team.tr; u < n; u += team.ts) {
+                    if (!d[u]) continue;
+                    int l = vl[u];
+                    for (int g = 0; g < n; g++) {
+                        const int ll = vl[l];
+                        if (ll >= l) break;
+                        l = ll;
+                    }
+                    vl[u] = l;
+                }
+                team.sync();
+            }
+            ok = conv;
+        }
+        if (!ok) dev_fail(A.status, A.abort_flag, DEV_UF_LIMIT, where_err + 3, q, algo);
+        if (threadIdx.x == 0) P.subtick(PROF_ICM_UNION);
+        const int root = (algo == ENGINE_ICM_UNION_FIND) ? uf_find(vl, seed) : vl[seed];
+        for (int u = team.tr; u < n; u += team.ts) {
+            if (!d[u]) continue;
+            const int lu = (algo == ENGINE_ICM_UNION_FIND) ? uf_find(vl, u) : vl[u];
+            if (lu != root) continue;
+            const int hu = D.has_h ? B.h[u] : 0;
+            int sa = 0, sb = 0;
+            if (locA) { sa = sA[u]; sA[u] = (int8_t)-sa; dEa -= 2 * sa * hu; }
+            if (locB) { sb = sB[u]; sB[u] = (int8_t)-sb; dEb -= 2 * sb * hu; }
+            const int e1 = B.row[u + 1];
+#pragma unroll 4
+            for (int a = B.row[u]; a < e1; a++) {
+                const uint32_t e = B.adj[a];
+                const int v = (int)(e >> 8);
+                const int J = (int)(int8_t)(e & 0xffu);
+                if (locA) atomicAdd(fA + v, J * (-2 * sa));
+                if (locB) atomicAdd(fB + v, J * (-2 * sb));
+                if (!d[v]) {
+                    const int sv = locA ? sA[v] : sB[v];
+                    if (locA) dEa -= 2 * J * sa * sv;
+                    if (locB) dEb -= 2 * J * sb * sv;
+                }
+            }
+        }
+        team.sync();
+    }
+    if (cnt > 0 && algo == ENGINE_ICM_BFS) {
         // breadth-first growth of the seed's cluster, flipping as it goes
         if (team.tr == 0) {
             X.queue[0] = seed;
@@ -346,6 +460,7 @@ __device__ void colored_sweep(const EngineArgs& A, const BlockCtx& B, unsigned l
                     acc_fl++;
                     const int dl = -2 * s;
                     const int e1 = row[i + 1];
+#pragma unroll 4
                     for (int a = row[i]; a < e1; a++) {
                         const uint32_t e = adj[a];
                         atomicAdd(fd + (e >> 8), (int)(int8_t)(e & 0xffu) * dl);

@@ -126,6 +126,11 @@ enum EngineFlags : int32_t {
     ENGINE_BEST_PER_PHASE = 1,    // track the best state after every colour phase
     ENGINE_REPLAY = 2,            // sequential sweep + traced decisions
     ENGINE_EXCHANGE_EVEN_ODD = 4, // deterministic even/odd exchange rounds
+    // cluster algorithm of the ICM phase (bits 3-4)
+    ENGINE_ICM_BFS = 0,
+    ENGINE_ICM_UNION_FIND = 8,
+    ENGINE_ICM_LABEL_PROP = 16,
+    ENGINE_ICM_MASK = 24,
 };
 
 enum PhaseBits : int32_t { PHASE_SWEEP = 1, PHASE_EXCHANGE = 2, PHASE_ICM = 4 };

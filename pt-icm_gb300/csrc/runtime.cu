@@ -218,12 +218,14 @@ int configure(pticm_ctx* c, bool replay) {
     };
     int rpc = (int)c->o.replicas_per_block;
     if (replay) rpc = R;
+    int dev = 0, sms = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     if (rpc <= 0) {
-        // one block per instance when the whole run is about one SM of work,
-        // otherwise one replica per block across the GPU
-        SmemPlan tmp;
-        const bool one_block_fits = fits(R, 1024, std::min(32, std::max(1, npairs)), false, tmp);
-        rpc = (one_block_fits && (int64_t)R * n <= 32768) ? R : 1;
+        // one replica per block (one SM each) while the replicas fit on the
+        // GPU at once; otherwise the smallest divisor of R that does
+        rpc = 1;
+        while (rpc < R && (R / rpc > sms || R % rpc != 0)) rpc++;
     }
     if (rpc <= 0 || R % rpc != 0) return fail(PTICM_ERR_INVALID, "replicas_per_block must divide the replica count");
     const int group = R / rpc;
@@ -231,7 +233,7 @@ int configure(pticm_ctx* c, bool replay) {
     if (replay) threads = std::min(1024, 32 * std::max(1, std::min(R, 32)));
     if (threads <= 0) {
         if (rpc > 1) threads = 1024;
-        else threads = std::min(1024, std::max(128, ((max_class * rpc + 31) / 32) * 32));
+        else threads = std::min(1024, std::max(128, ((std::max(max_class, n / 2) + 31) / 32) * 32));
     }
     if (threads % 32 != 0 || threads > 1024) return fail(PTICM_ERR_INVALID, "block_threads must be a multiple of 32, at most 1024");
     const bool block_team = (rpc == 1) && !replay;
@@ -252,9 +254,7 @@ int configure(pticm_ctx* c, bool replay) {
     c->block_team = block_team;
     c->plan = plan;
     if (group > 1) {
-        int dev = 0, sms = 0, per_sm = 0;
-        CK(cudaGetDevice(&dev));
-        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        int per_sm = 0;
         CK(engine_max_blocks_per_sm(replay, block_team, threads, plan.total, &per_sm));
         if ((int64_t)per_sm * sms < group)
             return fail(PTICM_ERR_UNSUPPORTED, "the replica blocks of one instance cannot all be resident (" +
@@ -304,7 +304,15 @@ EngineArgs make_args(pticm_ctx* c) {
     A.seed = c->o.seed;
     A.sm = c->plan;
     A.prof = (c->profiling && c->d_prof.n >= (size_t)c->group * PROF_PHASES) ? c->d_prof.p : nullptr;
-    A.flags = (c->o.best_per_phase ? ENGINE_BEST_PER_PHASE : 0) | (c->o.exchange == 1 ? ENGINE_EXCHANGE_EVEN_ODD : 0);
+    // automatic cluster search: label propagation on denser graphs, where
+    // overlap clusters are large and shallow; union-find on sparse ones
+    const double mean_deg = c->P.n ? (double)c->P.dadj.size() / (double)c->P.n : 0.0;
+    int algo = mean_deg >= 8.0 ? ENGINE_ICM_LABEL_PROP : ENGINE_ICM_UNION_FIND;
+    if (c->o.icm_algo == 1) algo = ENGINE_ICM_BFS;
+    else if (c->o.icm_algo == 2) algo = ENGINE_ICM_UNION_FIND;
+    else if (c->o.icm_algo == 3) algo = ENGINE_ICM_LABEL_PROP;
+    A.flags = (c->o.best_per_phase ? ENGINE_BEST_PER_PHASE : 0) | (c->o.exchange == 1 ? ENGINE_EXCHANGE_EVEN_ODD : 0) |
+              algo;
     return A;
 }
 
@@ -464,8 +472,9 @@ void pticm_opts_default(pticm_opts* o) {
     o->chains = 2;
     o->sweeps = 1;
     o->icm = 0;
-    o->exchange = 0;
-    o->best_per_phase = 1;
+    o->exchange = 1;
+    o->best_per_phase = 0;
+    o->icm_algo = 0;
 }
 
 int pticm_beta_linspace(double* beta, double T0, double T1, uint64_t nt, int inverse) {
@@ -480,6 +489,8 @@ int pticm_create(const pticm_problem* p, const pticm_opts* o, pticm_ctx** out) {
     if (o->chains < 1 || o->chains > 16) return fail(PTICM_ERR_INVALID, "chains must be in [1, 16]");
     if (o->icm && (o->chains % 2)) return fail(PTICM_ERR_INVALID, "ICM pairs chains: use an even chain count");
     if (o->sweeps < 1) return fail(PTICM_ERR_INVALID, "sweeps must be >= 1");
+    if (o->exchange > 1) return fail(PTICM_ERR_INVALID, "exchange must be 0 or 1");
+    if (o->icm_algo > 3) return fail(PTICM_ERR_INVALID, "icm_algo must be in 0..3");
     if (int rc = check_device()) return rc;
     auto c = std::make_unique<pticm_ctx>();
     c->P = p->hp;
@@ -653,7 +664,7 @@ int pticm_replay(pticm_ctx* c, const pticm_trace* t) {
     A.step0 = c->steps_done;
     A.nsteps = (int)steps;
     A.phase_mask = PHASE_SWEEP | PHASE_EXCHANGE | (c->nc ? PHASE_ICM : 0);
-    A.flags = ENGINE_REPLAY;
+    A.flags = ENGINE_REPLAY | (A.flags & ENGINE_ICM_MASK);
     A.replay.uniforms = d_u.p;
     A.replay.sweep_offsets = reinterpret_cast<const uint64_t*>(d_off.p);
     A.replay.xchg_slot = d_xs.p;

@@ -37,7 +37,7 @@ class ProblemInfo(C.Structure):
 class Opts(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("nt", C.c_uint32), ("chains", C.c_uint32), ("sweeps", C.c_uint32),
                 ("icm", C.c_uint32), ("exchange", C.c_uint32), ("best_per_phase", C.c_uint32),
-                ("block_threads", C.c_uint32), ("replicas_per_block", C.c_uint32)]
+                ("block_threads", C.c_uint32), ("replicas_per_block", C.c_uint32), ("icm_algo", C.c_uint32)]
 
 
 class Stats(C.Structure):
@@ -181,14 +181,14 @@ def beta_linspace(T0, T1, nt, inverse=False):
 class Context:
     """All replicas of one PT run resident on the current GPU."""
 
-    def __init__(self, problem: Problem, *, nt, chains=2, seed=0, sweeps=1, icm=True, exchange=0,
-                 best_per_phase=True, block_threads=0, replicas_per_block=0):
+    def __init__(self, problem: Problem, *, nt, chains=2, seed=0, sweeps=1, icm=True, exchange=1,
+                 best_per_phase=False, block_threads=0, replicas_per_block=0, icm_algo=0):
         L = lib()
         o = Opts()
         L.pticm_opts_default(C.byref(o))
         o.seed, o.nt, o.chains, o.sweeps, o.icm = seed, nt, chains, sweeps, int(icm)
         o.exchange, o.best_per_phase = exchange, int(best_per_phase)
-        o.block_threads, o.replicas_per_block = block_threads, replicas_per_block
+        o.block_threads, o.replicas_per_block, o.icm_algo = block_threads, replicas_per_block, icm_algo
         h = C.c_void_p()
         _check(L.pticm_create(problem._h, C.byref(o), C.byref(h)))
         self._h = h
@@ -276,7 +276,7 @@ class Context:
 
 
 def solve(problem: Problem, *, seed, Nt, pts, T0=0.6, T1=2.8, inverse=False, icm=False, sweeps=1,
-          ladder=None, chains=2, exchange=0, **kw):
+          ladder=None, chains=2, exchange=1, **kw):
     """The reference's solve() (src/solver.cc:16-166) on the GPU: linear-beta
     ladder (or `ladder`), Bernoulli initial states, `pts` PT steps.  Returns
     the keys src/solver.cc:151-163 prints."""

@@ -20,6 +20,7 @@
 #include "pticm.h"
 #include "pticm_engine.h"
 #include "problem_host.h"
+#include "runtime_internal.h"
 
 namespace pticm {
 cudaError_t launch_engine(const EngineArgs& A, int threads, bool replay, bool block_team, bool cooperative,
@@ -146,7 +147,7 @@ struct pticm_ctx {
     }
 };
 
-namespace {
+namespace pticm {
 
 // Shared-memory layout for a launch; every region starts on 16 bytes.
 SmemPlan make_plan(const InstanceDesc& D, bool replay, int teams, int threads, bool stage_adj) {
@@ -201,14 +202,15 @@ SmemPlan make_plan(const InstanceDesc& D, bool replay, int teams, int threads, b
     return S;
 }
 
-// Choose replicas per block, block size, ICM teams and the smem plan.
-int configure(pticm_ctx* c, bool replay) {
-    InstanceDesc& D = c->desc;
-    const int R = c->R, n = (int)c->P.n;
-    const int npairs = c->nc * (c->C / 2);
+// Choose replicas per block, block size, ICM teams and the smem plan for an
+// instance described by D (D.rpc / D.group are filled in).  Allocates
+// nothing: it only queries device attributes and occupancy.
+int choose_config(const HostProblem& P, const pticm_opts& o, bool replay, InstanceDesc& D, LaunchConfig& cfg,
+                  std::string& msg) {
+    const int R = D.R, n = (int)P.n;
+    const int npairs = D.nc * (D.chains / 2);
     int max_class = 1;
-    for (int k = 0; k < c->P.ncolors; k++)
-        max_class = std::max(max_class, c->P.color_off[k + 1] - c->P.color_off[k]);
+    for (int k = 0; k < P.ncolors; k++) max_class = std::max(max_class, P.color_off[k + 1] - P.color_off[k]);
     auto fits = [&](int rpc, int threads, int teams, bool stage, SmemPlan& out) {
         InstanceDesc t = D;
         t.rpc = rpc;
@@ -216,26 +218,30 @@ int configure(pticm_ctx* c, bool replay) {
         out = make_plan(t, replay, teams, threads, stage);
         return out.total <= kSmemLimit;
     };
-    int rpc = (int)c->o.replicas_per_block;
+    int rpc = (int)o.replicas_per_block;
     if (replay) rpc = R;
     int dev = 0, sms = 0;
-    CK(cudaGetDevice(&dev));
-    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) { msg = cudaGetErrorString(e); return PTICM_ERR_CUDA; }
     if (rpc <= 0) {
         // one replica per block (one SM each) while the replicas fit on the
         // GPU at once; otherwise the smallest divisor of R that does
         rpc = 1;
         while (rpc < R && (R / rpc > sms || R % rpc != 0)) rpc++;
     }
-    if (rpc <= 0 || R % rpc != 0) return fail(PTICM_ERR_INVALID, "replicas_per_block must divide the replica count");
+    if (rpc <= 0 || R % rpc != 0) { msg = "replicas_per_block must divide the replica count"; return PTICM_ERR_INVALID; }
     const int group = R / rpc;
-    int threads = (int)c->o.block_threads;
+    int threads = (int)o.block_threads;
     if (replay) threads = std::min(1024, 32 * std::max(1, std::min(R, 32)));
     if (threads <= 0) {
         if (rpc > 1) threads = 1024;
         else threads = std::min(1024, std::max(128, ((std::max(max_class, n / 2) + 31) / 32) * 32));
     }
-    if (threads % 32 != 0 || threads > 1024) return fail(PTICM_ERR_INVALID, "block_threads must be a multiple of 32, at most 1024");
+    if (threads % 32 != 0 || threads > 1024) {
+        msg = "block_threads must be a multiple of 32, at most 1024";
+        return PTICM_ERR_INVALID;
+    }
     const bool block_team = (rpc == 1) && !replay;
     int teams = block_team ? 1 : std::max(1, std::min(threads / 32, std::max(1, npairs)));
     SmemPlan plan;
@@ -243,27 +249,87 @@ int configure(pticm_ctx* c, bool replay) {
     while (!fits(rpc, threads, teams, stage, plan)) {
         if (stage) { stage = false; continue; }
         if (teams > 1) { teams = std::max(1, teams / 2); continue; }
-        return fail(PTICM_ERR_UNSUPPORTED, "the replicas of one block do not fit in shared memory; use fewer replicas per block");
+        msg = "the replicas of one block do not fit in shared memory; use fewer replicas per block";
+        return PTICM_ERR_UNSUPPORTED;
     }
     D.rpc = rpc;
     D.group = group;
-    c->rpc = rpc;
-    c->group = group;
-    c->threads = threads;
-    c->teams = teams;
-    c->block_team = block_team;
-    c->plan = plan;
+    cfg.rpc = rpc;
+    cfg.group = group;
+    cfg.threads = threads;
+    cfg.teams = teams;
+    cfg.block_team = block_team;
+    cfg.plan = plan;
     if (group > 1) {
         int per_sm = 0;
-        CK(engine_max_blocks_per_sm(replay, block_team, threads, plan.total, &per_sm));
-        if ((int64_t)per_sm * sms < group)
-            return fail(PTICM_ERR_UNSUPPORTED, "the replica blocks of one instance cannot all be resident (" +
-                                                   std::to_string(group) + " blocks, " + std::to_string(per_sm * sms) +
-                                                   " resident); raise replicas_per_block");
+        e = engine_max_blocks_per_sm(replay, block_team, threads, plan.total, &per_sm);
+        if (e != cudaSuccess) { msg = cudaGetErrorString(e); return PTICM_ERR_CUDA; }
+        if ((int64_t)per_sm * sms < group) {
+            msg = "the replica blocks of one instance cannot all be resident (" + std::to_string(group) +
+                  " blocks, " + std::to_string(per_sm * sms) + " resident); raise replicas_per_block";
+            return PTICM_ERR_UNSUPPORTED;
+        }
     }
-    std::vector<int32_t> bi(group, 0);
+    return PTICM_OK;
+}
+
+// Engine flags for the options: exchange order, best tracking, cluster search
+// (automatic: label propagation on denser graphs, where overlap clusters are
+// large and shallow; union-find on sparse ones).
+int engine_flags(const HostProblem& P, const pticm_opts& o) {
+    const double mean_deg = P.n ? (double)P.dadj.size() / (double)P.n : 0.0;
+    int algo = mean_deg >= 8.0 ? ENGINE_ICM_LABEL_PROP : ENGINE_ICM_UNION_FIND;
+    if (o.icm_algo == 1) algo = ENGINE_ICM_BFS;
+    else if (o.icm_algo == 2) algo = ENGINE_ICM_UNION_FIND;
+    else if (o.icm_algo == 3) algo = ENGINE_ICM_LABEL_PROP;
+    return (o.best_per_phase ? ENGINE_BEST_PER_PHASE : 0) | (o.exchange == 1 ? ENGINE_EXCHANGE_EVEN_ODD : 0) | algo;
+}
+
+// Acceptance tables of a ladder: thr = ceil(exp(-beta*dE) 2^32) (all-ones:
+// always) and the FP64 exp(-beta*dE) itself, dE = 2t, t = 1..kmax; and the
+// ICM pair count of src/initialization.cc:158-164 (nc < 0) or nc.
+int ladder_tables(const HostProblem& P, const double* beta, int nt, int nc_req, bool icm, int chains,
+                  std::vector<uint32_t>& thr, std::vector<double>& ptab) {
+    const int kst = P.kmax + 1;
+    thr.assign((size_t)nt * kst, 0xFFFFFFFFu);
+    ptab.assign((size_t)nt * kst, 1.0);
+    for (int k = 0; k < nt; k++)
+        for (int t = 1; t < kst; t++) {
+            const double dE = 2.0 * t;
+            const double p = std::exp(-beta[k] * dE);   // the reference's expression, src/replica.cc:35
+            ptab[(size_t)k * kst + t] = p;
+            const double scaled = std::ceil(p * 4294967296.0);
+            thr[(size_t)k * kst + t] = (p >= 1.0 || scaled >= 4294967295.0) ? 0xFFFFFFFFu : (uint32_t)scaled;
+        }
+    int count = 0;
+    if (nc_req >= 0) {
+        count = std::min(nc_req, nt);
+    } else {
+        for (int i = nt - 1; i >= 0; i--) {
+            if (beta[i] < P.char_scale) break;
+            count++;
+        }
+    }
+    return (icm && chains >= 2) ? count : 0;
+}
+
+}  // namespace pticm
+
+namespace {
+
+int configure(pticm_ctx* c, bool replay) {
+    std::string msg;
+    LaunchConfig cfg;
+    if (int rc = choose_config(c->P, c->o, replay, c->desc, cfg, msg)) return fail(rc, msg);
+    c->rpc = cfg.rpc;
+    c->group = cfg.group;
+    c->threads = cfg.threads;
+    c->teams = cfg.teams;
+    c->block_team = cfg.block_team;
+    c->plan = cfg.plan;
+    std::vector<int32_t> bi(cfg.group, 0);
     CK(c->d_block_inst.upload(bi));
-    CK(c->d_desc.upload(std::vector<InstanceDesc>{D}));
+    CK(c->d_desc.upload(std::vector<InstanceDesc>{c->desc}));
     return PTICM_OK;
 }
 
@@ -304,15 +370,7 @@ EngineArgs make_args(pticm_ctx* c) {
     A.seed = c->o.seed;
     A.sm = c->plan;
     A.prof = (c->profiling && c->d_prof.n >= (size_t)c->group * PROF_PHASES) ? c->d_prof.p : nullptr;
-    // automatic cluster search: label propagation on denser graphs, where
-    // overlap clusters are large and shallow; union-find on sparse ones
-    const double mean_deg = c->P.n ? (double)c->P.dadj.size() / (double)c->P.n : 0.0;
-    int algo = mean_deg >= 8.0 ? ENGINE_ICM_LABEL_PROP : ENGINE_ICM_UNION_FIND;
-    if (c->o.icm_algo == 1) algo = ENGINE_ICM_BFS;
-    else if (c->o.icm_algo == 2) algo = ENGINE_ICM_UNION_FIND;
-    else if (c->o.icm_algo == 3) algo = ENGINE_ICM_LABEL_PROP;
-    A.flags = (c->o.best_per_phase ? ENGINE_BEST_PER_PHASE : 0) | (c->o.exchange == 1 ? ENGINE_EXCHANGE_EVEN_ODD : 0) |
-              algo;
+    A.flags = engine_flags(c->P, c->o);
     return A;
 }
 
@@ -366,6 +424,11 @@ int reset_run_state(pticm_ctx* c) {
 }
 
 }  // namespace
+
+namespace pticm {
+const HostProblem& problem_host(const pticm_problem* p) { return p->hp; }
+void set_last_error(const std::string& m) { g_err = m; }
+}  // namespace pticm
 
 extern "C" {
 
@@ -552,28 +615,10 @@ int pticm_set_ladder(pticm_ctx* c, const double* beta, uint32_t nt, int32_t nc) 
     for (uint32_t k = 0; k < nt; k++)
         if (!std::isfinite(beta[k])) return fail(PTICM_ERR_INVALID, "non-finite inverse temperature");
     c->beta.assign(beta, beta + nt);
-    int count = 0;
-    if (nc >= 0) {
-        count = std::min<int>(nc, c->nt);
-    } else {
-        for (int i = c->nt - 1; i >= 0; i--) {
-            if (c->beta[i] < c->P.char_scale) break;
-            count++;
-        }
-    }
-    c->nc = (c->o.icm && c->C >= 2) ? count : 0;
+    std::vector<uint32_t> thr;
+    std::vector<double> ptab;
+    c->nc = ladder_tables(c->P, beta, c->nt, nc, c->o.icm != 0, c->C, thr, ptab);
     c->desc.nc = c->nc;
-    const int kst = c->P.kmax + 1;
-    std::vector<uint32_t> thr((size_t)c->nt * kst, 0xFFFFFFFFu);
-    std::vector<double> ptab((size_t)c->nt * kst, 1.0);
-    for (int k = 0; k < c->nt; k++)
-        for (int t = 1; t < kst; t++) {
-            const double dE = 2.0 * t;
-            const double p = std::exp(-c->beta[k] * dE);   // the reference's expression, src/replica.cc:35
-            ptab[(size_t)k * kst + t] = p;
-            const double scaled = std::ceil(p * 4294967296.0);
-            thr[(size_t)k * kst + t] = (p >= 1.0 || scaled >= 4294967295.0) ? 0xFFFFFFFFu : (uint32_t)scaled;
-        }
     CK(c->d_beta.upload(c->beta));
     CK(c->d_thr.upload(thr, 4));
     CK(c->d_ptab.upload(ptab, 4));

@@ -188,6 +188,44 @@ typedef struct pticm_trace {
 
 int pticm_replay(pticm_ctx* c, const pticm_trace* t);
 
+/* ----------------------------------------------- no device allocation -- */
+/* For callers that cannot call cudaMalloc (their host framework owns every
+ * device allocation and hands out buffers, or they must avoid the implicit
+ * synchronisation of cudaMalloc/cudaFree): a complete PT run of `pt_steps`
+ * steps (sweeps, exchange, ICM, as pticm_run) whose working memory lives in a
+ * fixed device array of PTICM_NOALLOC_SCRATCH_BYTES inside this library.
+ * This entry point has no counterpart in the reference.
+ *
+ * The caller passes device buffers for inputs and outputs (below); the run
+ * starts from `spins_in` (fields and energies are recomputed from them) and
+ * uses the steps step0..step0+pt_steps-1 of the counter-based random streams,
+ * so chaining calls with step0 advanced continues one trajectory.  It calls
+ * no cudaMalloc, cudaFree or allocating library routine.  Runs whose working
+ * set exceeds the array (about 11 bytes per replica-site plus the graph) are
+ * rejected with PTICM_ERR_UNSUPPORTED.  The first call on a device resolves
+ * the array's address (make it before any stream capture); every GPU that
+ * loads the library holds the array until exit; all calls share it, so calls
+ * that overlap on the GPU race. `stream` is a cudaStream_t (NULL = legacy
+ * default stream); the call returns after the stream has finished the run. */
+#define PTICM_NOALLOC_SCRATCH_BYTES (8u << 20)
+
+typedef struct pticm_noalloc_io {
+    const uint8_t* spins_in;     /* device, R*n bytes (0/1, original site order), */
+                                 /* replica r = chain*nt + k                     */
+    uint8_t* spins_out;          /* device, R*n bytes; may be spins_in           */
+    int64_t* energy_out;         /* device, R energies                           */
+    uint32_t* slot_to_replica;   /* device, R, in/out; NULL: identity start       */
+    uint32_t* pair_order;        /* device, nt-1, in/out (reference exchange     */
+                                 /* order); NULL: ascending start                */
+    uint64_t* swap_attempts;     /* device, R: this call's counts, or NULL        */
+    uint64_t* swap_successes;    /* device, R, or NULL                           */
+    int64_t* best_energy_out;    /* device, R: lowest energy seen this call, or NULL */
+    uint8_t* best_states_out;    /* device, R*n: the matching states, or NULL    */
+} pticm_noalloc_io;
+
+int pticm_run_noalloc(const pticm_problem* p, const pticm_opts* o, const double* beta, uint32_t nt, int32_t nc,
+                      const pticm_noalloc_io* io, uint64_t step0, uint64_t pt_steps, void* stream);
+
 /* ----------------------------------------------------------- utilities -- */
 const char* pticm_last_error(void);
 const char* pticm_version(void);

@@ -50,6 +50,18 @@ def _graph():
     return instances.c2()
 
 
+def _profiled_traffic():
+    """DRAM bytes per engine launch from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "pt_engine_c2_bench.md")) as f:
+            for line in f:
+                if line.startswith("| traffic_bytes_per_launch |"):
+                    return int(line.split("|")[2].strip())
+    except (OSError, ValueError):
+        pass
+    return None
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -283,9 +295,10 @@ def run_gpu(args):
                         "1000 PT steps + best state/statistics read back, per step"},
         "gpu_launches": args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak, "traffic": _profiled_traffic(),
                      "note": f"algorithmic bytes 2N+12M per replica-sweep; peak {peak_kind} HBM copy; "
-                             "data is shared-memory resident"},
+                             "data is shared-memory resident; traffic = ncu DRAM bytes per launch "
+                             "(profiles/pt_engine_c2_bench.md)"},
         "clocks": clk.summary(),
     }
     if not args.no_cpu_baseline:

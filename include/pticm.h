@@ -169,6 +169,37 @@ int pticm_verify(pticm_ctx* c, uint64_t* mismatches);
 int pticm_set_profiling(pticm_ctx* c, int enable);
 int pticm_get_profile(pticm_ctx* c, double* mean_ms, double* max_ms);
 
+/* -------------------------------------------- multihistogram ladder -- */
+/* get_beta (src/cae_estimator.cc:295-428) on the GPU: a pilot PT run
+ * (gather_samples, :76-151: one chain of nt temperatures linear in beta from
+ * max(beta(T0), beta(T1)) down, burn_in + samples steps, shuffled-order
+ * exchange, no ICM) with per-temperature energy histograms accumulated in the
+ * kernel, the FP64 multihistogram density of states (:155-253) on the GPU,
+ * and the greedy constant-acceptance walk to pair acceptance r (:367-425).
+ * beta_out (>= nt entries) receives the descending ladder, *count its length.
+ * The reference calls it with estep 2 and r 0.4 (src/initialization.cc:110)
+ * and a burn-in of 5000 (src/cae_estimator.cc:74). */
+int pticm_cae_ladder(const pticm_problem* p, uint64_t seed, double T0, double T1, int inverse, uint32_t nt,
+                     double estep, double step_size, double r, uint64_t samples, uint64_t burn_in,
+                     double* beta_out, uint32_t* count);
+
+/* The multihistogram fixed point alone (get_partition_iterate,
+ * src/cae_estimator.cc:228-253) for caller histograms in make_histogram's
+ * layout (:45-69): row j has hist_len[j] counts at hist_off[j], bin 0 at
+ * energy emin[j], bin width estep; n samples per row.  Writes
+ * nbins = ceil((max_emax - min_j emin[j]) / estep) values of ln g (up to
+ * logdos_cap) and the nt values of ln Z; iterates until
+ * sum_j ((lnZ_j - lnZ'_j) / lnZ'_j)^2 <= 1e-7. */
+int pticm_mhist_dos(const uint32_t* hist, const uint64_t* hist_off, const uint64_t* hist_len, uint32_t nt,
+                    const double* beta_hist, const double* emin, double estep, uint64_t n, double max_emax,
+                    double* logdos, uint64_t logdos_cap, double* logZ, uint64_t* nbins, uint64_t* iterations);
+
+/* The constant-acceptance walk alone (src/cae_estimator.cc:367-425) from a
+ * density of states; host code (no GPU needed), O(nbins) per candidate. */
+int pticm_cae_walk(const double* logdos, uint64_t nbins, double min_emin, double estep, double beta_start,
+                   double beta_end, double step_size, double r, uint32_t num_temps, double* beta_out,
+                   uint32_t* count);
+
 /* --------------------------------------------------------------- replay -- */
 /* The reference's sequential algorithm driven by a recorded trace of its
  * random decisions: per PT step, per sweep, per replica the uniforms

@@ -973,12 +973,21 @@ uint64_t orc_cae_walk(const double* logdos, uint64_t nb, double min_emin, double
     return walk_ladder(logdos, nb, min_emin, estep, beta_start, beta_end, step_size, r, num_temps, beta_out);
 }
 
+/* The pilot run of gather_samples (:76-151) on hist_betas hb[0..Nt) and the
+ * per-temperature histograms of make_histogram (:45-69).  Returns a malloc'd
+ * concatenation of the histograms (row j at hoff[j], length hlen[j]); emin_v,
+ * emaxv receive each row's energy range and *n_out the int-accumulated count
+ * of row 0 (src/cae_estimator.cc:343). */
+static uint32_t* pilot_histograms(orc_problem* p, const double* hb, uint64_t Nt, double estep,
+                                  uint64_t num_samples, uint64_t burn_in, uint64_t* hoff, uint64_t* hlen,
+                                  double* emin_v, double* emaxv, uint64_t* n_out);
+
 /* gather_samples (:76-151) + make_histogram (:45-69) + get_beta (:295-428) */
 uint64_t orc_get_beta(orc_problem* p, double T0, double T1, int inverse, uint64_t num_temps,
                       double estep, double step_size, double r, uint64_t num_samples,
                       uint64_t burn_in, double* beta_out,
                       double* hist_betas_out, double* emin_out, double* emax_out) {
-    uint64_t Nt = num_temps, N = (uint64_t)p->n;
+    uint64_t Nt = num_temps;
     double beta_start, beta_end;
     if (inverse) { beta_start = T0; beta_end = T1; }
     else { beta_start = 1 / T0; beta_end = 1 / T1; }
@@ -987,6 +996,43 @@ uint64_t orc_get_beta(orc_problem* p, double T0, double T1, int inverse, uint64_
     double* hb = (double*)malloc(Nt * sizeof(double));
     double beta = beta_start;
     for (uint64_t i = 0; i < Nt; i++, beta += beta_step) hb[i] = beta;
+    uint64_t* hoff = (uint64_t*)malloc(Nt * sizeof(uint64_t));
+    uint64_t* hlen = (uint64_t*)malloc(Nt * sizeof(uint64_t));
+    double* emin_v = (double*)malloc(Nt * sizeof(double));
+    double* emaxv = (double*)malloc(Nt * sizeof(double));
+    uint64_t n = 0;
+    uint32_t* hist = pilot_histograms(p, hb, Nt, estep, num_samples, burn_in, hoff, hlen, emin_v, emaxv, &n);
+    double max_emax = -DBL_MAX, min_emin = DBL_MAX;
+    for (uint64_t i = 0; i < Nt; i++) {
+        if (emaxv[i] > max_emax) max_emax = emaxv[i];
+        if (emin_v[i] < min_emin) min_emin = emin_v[i];
+    }
+    uint64_t nb = (uint64_t)ceil((max_emax - min_emin) / estep);
+    double* logdos = (double*)malloc((nb ? nb : 1) * sizeof(double));
+    double* pf = (double*)malloc(Nt * sizeof(double));
+    orc_partition_iterate(hist, hoff, hlen, Nt, hb, emin_v, estep, n, max_emax, logdos, pf);
+    uint64_t cnt = walk_ladder(logdos, nb, min_emin, estep, beta_start, beta_end, step_size, r, Nt, beta_out);
+    if (hist_betas_out) memcpy(hist_betas_out, hb, Nt * sizeof(double));
+    if (emin_out) memcpy(emin_out, emin_v, Nt * sizeof(double));
+    if (emax_out) memcpy(emax_out, emaxv, Nt * sizeof(double));
+    free(hb); free(hoff); free(hlen); free(emin_v); free(emaxv); free(hist); free(logdos); free(pf);
+    return cnt;
+}
+
+uint64_t orc_pilot(orc_problem* p, const double* hb, uint64_t Nt, double estep, uint64_t num_samples,
+                   uint64_t burn_in, uint32_t* hist_out, uint64_t hist_cap, uint64_t* hoff, uint64_t* hlen,
+                   double* emin_v, double* emaxv, uint64_t* n_out) {
+    uint32_t* h = pilot_histograms(p, hb, Nt, estep, num_samples, burn_in, hoff, hlen, emin_v, emaxv, n_out);
+    uint64_t tot = hoff[Nt - 1] + hlen[Nt - 1];
+    if (hist_out) memcpy(hist_out, h, (tot < hist_cap ? tot : hist_cap) * sizeof(uint32_t));
+    free(h);
+    return tot;
+}
+
+static uint32_t* pilot_histograms(orc_problem* p, const double* hb, uint64_t Nt, double estep,
+                                  uint64_t num_samples, uint64_t burn_in, uint64_t* hoff, uint64_t* hlen,
+                                  double* emin_v, double* emaxv, uint64_t* n_out) {
+    uint64_t N = (uint64_t)p->n;
     /* pilot run */
     uint8_t* s = (uint8_t*)malloc(Nt * N);
     double* dE = (double*)malloc(Nt * N * sizeof(double));
@@ -1028,12 +1074,7 @@ uint64_t orc_get_beta(orc_problem* p, double T0, double T1, int inverse, uint64_
         }
     }
     /* histograms per temperature slot */
-    double* emin_v = (double*)malloc(Nt * sizeof(double));
-    uint64_t* hoff = (uint64_t*)malloc(Nt * sizeof(uint64_t));
-    uint64_t* hlen = (uint64_t*)malloc(Nt * sizeof(uint64_t));
-    double max_emax = -DBL_MAX, min_emin = DBL_MAX;
     uint64_t tot = 0;
-    double* emaxv = (double*)malloc(Nt * sizeof(double));
     for (uint64_t i = 0; i < Nt; i++) {
         double* lg = logs + i * num_samples;
         double mn = lg[0], mx = lg[0];
@@ -1042,8 +1083,6 @@ uint64_t orc_get_beta(orc_problem* p, double T0, double T1, int inverse, uint64_
         hlen[i] = (uint64_t)ceil((mx - mn) / estep) + 1;
         hoff[i] = tot;
         tot += hlen[i];
-        if (mx > max_emax) max_emax = mx;
-        if (mn < min_emin) min_emin = mn;
     }
     uint32_t* hist = (uint32_t*)calloc(tot ? tot : 1, sizeof(uint32_t));
     for (uint64_t i = 0; i < Nt; i++) {
@@ -1053,16 +1092,7 @@ uint64_t orc_get_beta(orc_problem* p, double T0, double T1, int inverse, uint64_
     /* n = accumulate(histograms[0]) with an int accumulator */
     int32_t nacc = 0;
     for (uint64_t b = 0; b < hlen[0]; b++) nacc = (int32_t)(nacc + (int32_t)hist[hoff[0] + b]);
-    uint64_t n = (uint64_t)(int64_t)nacc;
-    uint64_t nb = (uint64_t)ceil((max_emax - min_emin) / estep);
-    double* logdos = (double*)malloc((nb ? nb : 1) * sizeof(double));
-    double* pf = (double*)malloc(Nt * sizeof(double));
-    orc_partition_iterate(hist, hoff, hlen, Nt, hb, emin_v, estep, n, max_emax, logdos, pf);
-    uint64_t cnt = walk_ladder(logdos, nb, min_emin, estep, beta_start, beta_end, step_size, r, Nt, beta_out);
-    if (hist_betas_out) memcpy(hist_betas_out, hb, Nt * sizeof(double));
-    if (emin_out) memcpy(emin_out, emin_v, Nt * sizeof(double));
-    if (emax_out) memcpy(emax_out, emaxv, Nt * sizeof(double));
-    free(hb); free(s); free(dE); free(E); free(rb); free(bE); free(bS); free(ctr); free(order); free(ri);
-    free(logs); free(emin_v); free(hoff); free(hlen); free(emaxv); free(hist); free(logdos); free(pf);
-    return cnt;
+    *n_out = (uint64_t)(int64_t)nacc;
+    free(s); free(dE); free(E); free(rb); free(bE); free(bS); free(ctr); free(order); free(ri); free(logs);
+    return hist;
 }

@@ -172,6 +172,12 @@ uint64_t orc_get_beta(orc_problem* p, double T0, double T1, int inverse, uint64_
                       uint64_t burn_in, double* beta_out,
                       double* hist_betas_out, double* emin_out, double* emax_out);
 
+/* The pilot run and histograms of get_beta on a given hist_betas ladder:
+ * writes up to hist_cap counts, returns the total; see orc_get_beta. */
+uint64_t orc_pilot(orc_problem* p, const double* hist_betas, uint64_t nt, double estep, uint64_t num_samples,
+                   uint64_t burn_in, uint32_t* hist_out, uint64_t hist_cap, uint64_t* hist_off, uint64_t* hist_len,
+                   double* emin, double* emax, uint64_t* n_out);
+
 #ifdef __cplusplus
 }
 #endif

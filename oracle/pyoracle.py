@@ -113,6 +113,8 @@ def lib():
         L.orc_get_beta.argtypes = [P, C.c_double, C.c_double, C.c_int, C.c_uint64, C.c_double,
                                    C.c_double, C.c_double, C.c_uint64, C.c_uint64, P, P, P, P]
         L.orc_get_beta.restype = C.c_uint64
+        L.orc_pilot.argtypes = [P, P, C.c_uint64, C.c_double, C.c_uint64, C.c_uint64, P, C.c_uint64, P, P, P, P, P]
+        L.orc_pilot.restype = C.c_uint64
         _lib = L
     return _lib
 
@@ -292,6 +294,48 @@ def get_beta(prob: Problem, *, seed, T0, T1, Nt, inverse=False, estep=2.0, step_
     cnt = L.orc_get_beta(prob.h, T0, T1, int(inverse), Nt, estep, step_size, r, samples, burn_in,
                          _p(out), _p(hb), _p(emn), _p(emx))
     return dict(count=cnt, beta=out[:cnt], hist_betas=hb, emin=emn, emax=emx)
+
+
+def pilot(prob: Problem, *, seed, hist_betas, estep=2.0, samples=2000, burn_in=5000):
+    """The pilot run and histograms of get_beta (src/cae_estimator.cc:76-151,
+    45-69) on the given hist_betas."""
+    L = lib()
+    L.orc_mt64_seed(prob.rng(), seed)
+    hb = np.ascontiguousarray(hist_betas, np.float64)
+    nt = len(hb)
+    off = np.zeros(nt, np.uint64)
+    ln = np.zeros(nt, np.uint64)
+    emn = np.zeros(nt)
+    emx = np.zeros(nt)
+    n = C.c_uint64()
+    cap = 1 << 24
+    h = np.zeros(cap, np.uint32)
+    tot = L.orc_pilot(prob.h, _p(hb), nt, estep, samples, burn_in, _p(h), cap, _p(off), _p(ln), _p(emn), _p(emx),
+                      C.byref(n))
+    return dict(hist=h[:tot].copy(), hist_off=off, hist_len=ln, emin=emn, emax=emx, n=n.value, hist_betas=hb)
+
+
+def partition_iterate(hist, hist_off, hist_len, beta_hist, emin, estep, n, max_emax):
+    """get_partition_iterate (src/cae_estimator.cc:228-253): (ln g, ln Z)."""
+    L = lib()
+    nt = len(beta_hist)
+    nb = int(np.ceil((max_emax - np.min(emin)) / estep))
+    dos = np.zeros(max(nb, 1))
+    z = np.zeros(nt)
+    hist = np.ascontiguousarray(hist, np.uint32)
+    off = np.ascontiguousarray(hist_off, np.uint64)
+    ln = np.ascontiguousarray(hist_len, np.uint64)
+    b = np.ascontiguousarray(beta_hist, np.float64)
+    e = np.ascontiguousarray(emin, np.float64)
+    it = L.orc_partition_iterate(_p(hist), _p(off), _p(ln), nt, _p(b), _p(e), estep, n, max_emax, _p(dos), _p(z))
+    return dos[:nb], z, it
+
+
+def cae_walk(logdos, min_emin, estep, beta_start, beta_end, step_size, r, num_temps):
+    d = np.ascontiguousarray(logdos, np.float64)
+    out = np.zeros(num_temps)
+    cnt = lib().orc_cae_walk(_p(d), len(d), min_emin, estep, beta_start, beta_end, step_size, r, num_temps, _p(out))
+    return out[:cnt]
 
 
 # ----------------------------------------------------------- reference runs

@@ -949,6 +949,13 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
             __syncthreads();
         }
         P.tick(PROF_BARRIER);
+        if (A.hist != nullptr && step >= A.hist_from && B.rank == 0) {
+            for (int k = tid; k < R; k += T) {
+                const long long bin = (B.E[B.slot[k]] - A.hist_lo) >> 1;
+                if (bin >= 0 && bin < A.hist_nbins) atomicAdd(A.hist + (long long)k * A.hist_nbins + bin, 1u);
+            }
+            __syncthreads();
+        }
         if (A.phase_mask & PHASE_EXCHANGE) {
             if (REPLAY) exchange_replay(A, B, ls, s_beta, s_att, s_succ);
             else if (A.flags & ENGINE_EXCHANGE_EVEN_ODD) exchange_even_odd(A, B, step, s_dbeta, s_att, s_succ);

@@ -118,6 +118,13 @@ struct EngineArgs {
     int32_t flags;                // ENGINE_* flags
     unsigned long long seed;
     unsigned long long* prof;     // optional: per block, clock64 cycles per phase (PROF_PHASES)
+    // optional per-slot energy histograms (the pilot run of the multihistogram
+    // ladder): after the sweeps of every step >= hist_from, slot k counts the
+    // energy E of its replica in bin (E - hist_lo) / 2 of row k
+    unsigned int* hist;
+    long long hist_lo;
+    long long hist_nbins;
+    unsigned long long hist_from;
     SmemPlan sm;
     ReplayArgs replay;
 };

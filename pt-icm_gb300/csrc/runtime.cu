@@ -21,6 +21,7 @@
 #include "pticm_engine.h"
 #include "problem_host.h"
 #include "runtime_internal.h"
+#include "mhist_host.h"
 
 namespace pticm {
 cudaError_t launch_engine(const EngineArgs& A, int threads, bool replay, bool block_team, bool cooperative,
@@ -136,6 +137,9 @@ struct pticm_ctx {
     DArr<long long> d_E, d_Epub, d_bestE;
     DArr<unsigned long long> d_flips, d_bestSweep, d_att, d_succ, d_mismatch, d_prof;
     bool profiling = false;
+    DArr<unsigned int> d_hist;   // pilot energy histograms (multihistogram ladder)
+    long long hist_lo = 0, hist_nbins = 0;
+    uint64_t hist_from = 0;
     DArr<unsigned int> d_bar;
     DArr<int> d_abort;
     DArr<DevStatus> d_status;
@@ -370,6 +374,10 @@ EngineArgs make_args(pticm_ctx* c) {
     A.seed = c->o.seed;
     A.sm = c->plan;
     A.prof = (c->profiling && c->d_prof.n >= (size_t)c->group * PROF_PHASES) ? c->d_prof.p : nullptr;
+    A.hist = c->d_hist.p;
+    A.hist_lo = c->hist_lo;
+    A.hist_nbins = c->hist_nbins;
+    A.hist_from = c->hist_from;
     A.flags = engine_flags(c->P, c->o);
     return A;
 }
@@ -420,6 +428,59 @@ int reset_run_state(pticm_ctx* c) {
     c->steps_done = 0;
     c->attempts = 0;
     c->states_set = true;
+    return PTICM_OK;
+}
+
+}  // namespace
+
+namespace pticm {
+cudaError_t mhist_iterate(const uint32_t* hist, const uint64_t* hoff, const uint64_t* hlen, const double* emin,
+                          const double* beta, double* logZ, int nt, double estep, double min_emin, double logn,
+                          long long nbins, double* logdos, double* pmax, double* psum, int chunks, double* metric,
+                          cudaStream_t st);
+}  // namespace pticm
+
+namespace {
+
+// The multihistogram fixed point on the GPU (src/cae_estimator.cc:228-253):
+// iterate until sum_j ((lnZ_j - lnZ'_j)/lnZ'_j)^2 <= 1e-7, as the reference.
+int mhist_dos_impl(const uint32_t* hist, const uint64_t* hoff, const uint64_t* hlen, uint32_t nt,
+                   const double* beta, const double* emin, double estep, uint64_t n, double max_emax,
+                   std::vector<double>& logdos, std::vector<double>& logZ, double& min_emin, uint64_t& iters) {
+    if (nt < 1 || n == 0 || !(estep > 0)) return fail(PTICM_ERR_INVALID, "multihistogram needs samples, rows and estep > 0");
+    min_emin = emin[0];
+    for (uint32_t j = 1; j < nt; j++) min_emin = std::min(min_emin, emin[j]);
+    const long long nbins = (long long)std::ceil((max_emax - min_emin) / estep);
+    logdos.assign((size_t)std::max<long long>(nbins, 0), -DBL_MAX);
+    logZ.assign(nt, 0.0);
+    iters = 0;
+    if (nbins <= 0) return PTICM_OK;
+    const uint64_t total = hoff[nt - 1] + hlen[nt - 1];
+    DArr<uint32_t> d_hist;
+    DArr<uint64_t> d_off, d_len;
+    DArr<double> d_emin, d_beta, d_logZ, d_dos, d_pmax, d_psum, d_metric;
+    CK(d_hist.upload(std::vector<uint32_t>(hist, hist + total)));
+    CK(d_off.upload(std::vector<uint64_t>(hoff, hoff + nt)));
+    CK(d_len.upload(std::vector<uint64_t>(hlen, hlen + nt)));
+    CK(d_emin.upload(std::vector<double>(emin, emin + nt)));
+    CK(d_beta.upload(std::vector<double>(beta, beta + nt)));
+    CK(d_logZ.upload(logZ));
+    CK(d_dos.alloc((size_t)nbins));
+    const int chunks = (int)std::max<long long>(1, std::min<long long>(64, nbins / 2048));
+    CK(d_pmax.alloc((size_t)nt * chunks));
+    CK(d_psum.alloc((size_t)nt * chunks));
+    CK(d_metric.alloc(1));
+    const double logn = std::log((double)n);
+    for (uint64_t it = 0; it < 1000000; it++) {
+        CK(mhist_iterate(d_hist.p, d_off.p, d_len.p, d_emin.p, d_beta.p, d_logZ.p, (int)nt, estep, min_emin, logn,
+                         nbins, d_dos.p, d_pmax.p, d_psum.p, chunks, d_metric.p, nullptr));
+        double metric = 0;
+        CK(cudaMemcpy(&metric, d_metric.p, sizeof(double), cudaMemcpyDeviceToHost));
+        iters = it + 1;
+        if (!(metric > 1e-7)) break;
+    }
+    CK(d_dos.download(logdos));
+    CK(d_logZ.download(logZ));
     return PTICM_OK;
 }
 
@@ -865,6 +926,106 @@ int pticm_get_profile(pticm_ctx* c, double* mean_ms, double* max_ms) {
         if (mean_ms) mean_ms[q] = sum / blocks;
         if (max_ms) max_ms[q] = mx;
     }
+    return PTICM_OK;
+}
+
+int pticm_mhist_dos(const uint32_t* hist, const uint64_t* hist_off, const uint64_t* hist_len, uint32_t nt,
+                    const double* beta_hist, const double* emin, double estep, uint64_t n, double max_emax,
+                    double* logdos, uint64_t logdos_cap, double* logZ, uint64_t* nbins, uint64_t* iterations) {
+    if (!hist || !hist_off || !hist_len || !beta_hist || !emin || !nbins) return fail(PTICM_ERR_INVALID, "null argument");
+    if (int rc = check_device()) return rc;
+    std::vector<double> dos, z;
+    double min_emin = 0;
+    uint64_t it = 0;
+    if (int rc = mhist_dos_impl(hist, hist_off, hist_len, nt, beta_hist, emin, estep, n, max_emax, dos, z, min_emin, it))
+        return rc;
+    *nbins = dos.size();
+    if (logdos) std::copy(dos.begin(), dos.begin() + std::min<uint64_t>(logdos_cap, dos.size()), logdos);
+    if (logZ) std::copy(z.begin(), z.end(), logZ);
+    if (iterations) *iterations = it;
+    return PTICM_OK;
+}
+
+int pticm_cae_walk(const double* logdos, uint64_t nbins, double min_emin, double estep, double beta_start,
+                   double beta_end, double step_size, double r, uint32_t num_temps, double* beta_out, uint32_t* count) {
+    if (!logdos || !beta_out || !count || num_temps < 1) return fail(PTICM_ERR_INVALID, "invalid arguments");
+    std::vector<double> dos(logdos, logdos + nbins);
+    *count = cae_walk(dos, min_emin, estep, beta_start, beta_end, step_size, r, num_temps, beta_out);
+    return PTICM_OK;
+}
+
+int pticm_cae_ladder(const pticm_problem* p, uint64_t seed, double T0, double T1, int inverse, uint32_t nt,
+                     double estep, double step_size, double r, uint64_t samples, uint64_t burn_in,
+                     double* beta_out, uint32_t* count) {
+    if (!p || !beta_out || !count || nt < 2 || samples == 0 || !(estep > 0))
+        return fail(PTICM_ERR_INVALID, "invalid arguments");
+    if (int rc = check_device()) return rc;
+    const HostProblem& P = p->hp;
+    // histogram temperatures: linear in beta from the largest beta down
+    // (src/cae_estimator.cc:308-328)
+    double beta_start = inverse ? T0 : 1 / T0, beta_end = inverse ? T1 : 1 / T1;
+    if (beta_start < beta_end) std::swap(beta_start, beta_end);
+    const double beta_step = (beta_end - beta_start) / (double)(nt - 1);
+    std::vector<double> hb(nt);
+    double b = beta_start;
+    for (uint32_t i = 0; i < nt; i++, b += beta_step) hb[i] = b;
+    // pilot run (gather_samples, :76-151): one chain, no ICM, shuffled-order exchange
+    pticm_opts o;
+    pticm_opts_default(&o);
+    o.seed = seed;
+    o.nt = nt;
+    o.chains = 1;
+    o.icm = 0;
+    o.exchange = 0;
+    pticm_ctx* c = nullptr;
+    if (int rc = pticm_create(p, &o, &c)) return rc;
+    std::unique_ptr<pticm_ctx> hold(c);
+    if (int rc = pticm_set_ladder(c, hb.data(), nt, 0)) return rc;
+    // every energy lies in [-W, W], W = sum |J| over edges + sum |h|, and has
+    // the parity of W: bins of width 2 from -W are exact energy levels
+    long long directed = 0, lin = 0;
+    for (int64_t i = 0; i < P.n; i++) {
+        lin += std::llabs((long long)P.h[i]);
+        for (int64_t a = P.row[i]; a < P.row[i + 1]; a++) directed += std::llabs((long long)P.w[a]);
+    }
+    const long long wabs = directed / 2 + lin;
+    c->hist_lo = -wabs;
+    c->hist_nbins = wabs + 1;
+    c->hist_from = burn_in;
+    CK(c->d_hist.alloc((size_t)nt * (size_t)c->hist_nbins));
+    if (int rc = pticm_init_states(c, seed)) return rc;
+    if (int rc = pticm_run(c, burn_in + samples, 7)) return rc;
+    std::vector<unsigned> habs;
+    CK(c->d_hist.download(habs));
+    // per-temperature histograms over [emin_j, emax_j] with bin width estep
+    // (make_histogram, :45-69)
+    std::vector<uint64_t> hoff(nt), hlen(nt);
+    std::vector<double> emin(nt), emax(nt);
+    std::vector<uint32_t> hist;
+    for (uint32_t j = 0; j < nt; j++) {
+        const unsigned* row = habs.data() + (size_t)j * c->hist_nbins;
+        long long first = -1, last = -1;
+        for (long long bb = 0; bb < c->hist_nbins; bb++)
+            if (row[bb]) { if (first < 0) first = bb; last = bb; }
+        if (first < 0) return fail(PTICM_ERR_DEVICE, "pilot run recorded no energies");
+        emin[j] = (double)(c->hist_lo + 2 * first);
+        emax[j] = (double)(c->hist_lo + 2 * last);
+        hlen[j] = (uint64_t)std::ceil((emax[j] - emin[j]) / estep) + 1;
+        hoff[j] = hist.size();
+        hist.resize(hist.size() + hlen[j], 0);
+        for (long long bb = first; bb <= last; bb++)
+            if (row[bb]) hist[hoff[j] + (uint64_t)std::floor(((double)(c->hist_lo + 2 * bb) - emin[j]) / estep)] += row[bb];
+    }
+    int32_t nacc = 0;   // the reference accumulates row 0 into an int
+    for (uint64_t k = 0; k < hlen[0]; k++) nacc = (int32_t)(nacc + (int32_t)hist[hoff[0] + k]);
+    const double max_emax = *std::max_element(emax.begin(), emax.end());
+    std::vector<double> dos, z;
+    double min_emin = 0;
+    uint64_t it = 0;
+    if (int rc = mhist_dos_impl(hist.data(), hoff.data(), hlen.data(), nt, hb.data(), emin.data(), estep,
+                                (uint64_t)(int64_t)nacc, max_emax, dos, z, min_emin, it))
+        return rc;
+    *count = cae_walk(dos, min_emin, estep, beta_start, beta_end, step_size, r, nt, beta_out);
     return PTICM_OK;
 }
 

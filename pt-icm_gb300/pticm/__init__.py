@@ -86,6 +86,9 @@ def lib():
         "pticm_replay": [P, C.POINTER(Trace)],
         "pticm_philox_probe": [P, P, P, C.c_int],
         "pticm_set_profiling": [P, C.c_int],
+        "pticm_cae_ladder": [P, u64, dbl, dbl, C.c_int, u32, dbl, dbl, dbl, u64, u64, P, P],
+        "pticm_mhist_dos": [P, P, P, u32, P, P, dbl, u64, dbl, P, u64, P, P, P],
+        "pticm_cae_walk": [P, u64, dbl, dbl, dbl, dbl, dbl, dbl, u32, P, P],
         "pticm_get_profile": [P, P, P],
     }
     for name, args in sigs.items():
@@ -170,6 +173,45 @@ class Problem:
         dE = np.zeros((cnt, n)) if with_dE else None
         _check(lib().pticm_problem_evaluate(self._h, cnt, _p(s), _p(E), _p(cut), _p(dE)))
         return (E, cut, dE) if with_dE else (E, cut)
+
+
+def cae_ladder(problem: Problem, *, seed, T0, T1, nt, inverse=False, estep=2.0, step_size=0.1, r=0.4,
+               samples=2000, burn_in=5000):
+    """get_beta (src/cae_estimator.cc:295-428) on the GPU: the multihistogram
+    constant-acceptance ladder, descending in beta."""
+    out = np.zeros(nt)
+    cnt = C.c_uint32()
+    _check(lib().pticm_cae_ladder(problem._h, seed, T0, T1, int(inverse), nt, estep, step_size, r, samples,
+                                  burn_in, _p(out), C.byref(cnt)))
+    return out[:cnt.value]
+
+
+def mhist_dos(hist, hist_off, hist_len, beta_hist, emin, estep, n, max_emax):
+    """The FP64 multihistogram fixed point on the GPU: (ln g, ln Z, iterations)."""
+    hist = np.ascontiguousarray(hist, np.uint32)
+    off = np.ascontiguousarray(hist_off, np.uint64)
+    ln = np.ascontiguousarray(hist_len, np.uint64)
+    b = np.ascontiguousarray(beta_hist, np.float64)
+    e = np.ascontiguousarray(emin, np.float64)
+    nt = len(b)
+    cap = int(np.ceil((max_emax - e.min()) / estep)) + 1
+    dos = np.zeros(max(cap, 1))
+    z = np.zeros(nt)
+    nb = C.c_uint64()
+    it = C.c_uint64()
+    _check(lib().pticm_mhist_dos(_p(hist), _p(off), _p(ln), nt, _p(b), _p(e), estep, n, max_emax, _p(dos), cap,
+                                 _p(z), C.byref(nb), C.byref(it)))
+    return dos[:nb.value], z, it.value
+
+
+def cae_walk(logdos, min_emin, estep, beta_start, beta_end, step_size, r, num_temps):
+    """The constant-acceptance walk (host code)."""
+    d = np.ascontiguousarray(logdos, np.float64)
+    out = np.zeros(num_temps)
+    cnt = C.c_uint32()
+    _check(lib().pticm_cae_walk(_p(d), len(d), min_emin, estep, beta_start, beta_end, step_size, r, num_temps,
+                                _p(out), C.byref(cnt)))
+    return out[:cnt.value]
 
 
 def beta_linspace(T0, T1, nt, inverse=False):

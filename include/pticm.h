@@ -122,6 +122,11 @@ int pticm_init_states(pticm_ctx* c, uint64_t seed);
 /* Explicit initial spins: R*n bytes (0/1), replica r = chain*nt + k. */
 int pticm_set_states(pticm_ctx* c, const uint8_t* states);
 
+#define PTICM_PHASE_SWEEP 1u
+#define PTICM_PHASE_EXCHANGE 2u
+#define PTICM_PHASE_ICM 4u
+#define PTICM_PHASE_ALL 7u
+
 /* The PT loop (src/solver.cc:67-127): `pt_steps` steps of sweeps, exchange
  * and ICM. `phase_mask` selects phases (1 sweep, 2 exchange, 4 ICM; 7 = all)
  * so that each phase can be checked on its own. */
@@ -168,6 +173,16 @@ int pticm_verify(pticm_ctx* c, uint64_t* mismatches);
 #define PTICM_PROFILE_SLOTS 14
 int pticm_set_profiling(pticm_ctx* c, int enable);
 int pticm_get_profile(pticm_ctx* c, double* mean_ms, double* max_ms);
+
+/* Per-temperature energy histograms (the observables the reference's --log
+ * path was to log, src/main.cc:490-530, and the multihistogram input): from PT
+ * step `from_step` on, every step adds the energy of the replica at each slot
+ * after its sweeps, in exact levels E = e_lo + 2*bin (every energy has the
+ * parity of e_lo).  Enabling clears the counts. */
+int pticm_enable_energy_histograms(pticm_ctx* c, uint64_t from_step);
+/* Rows of slot k at hist[k*nbins ...] (R rows); pass hist = NULL to query
+ * nbins and e_lo first. */
+int pticm_get_energy_histograms(pticm_ctx* c, uint32_t* hist, int64_t* e_lo, uint64_t* nbins);
 
 /* -------------------------------------------- multihistogram ladder -- */
 /* get_beta (src/cae_estimator.cc:295-428) on the GPU: a pilot PT run

@@ -517,7 +517,7 @@ struct orc_trace {
     vec_t xlu;      /* double  : log(u) of each exchange attempt             */
     vec_t icm;      /* int64   : ICM seed site, -1 when the pair is equal    */
     vec_t init;     /* uint8   : initial states, replica-major               */
-    vec_t energy;   /* double  : energies after each PT step                 */
+    vec_t energy;   /* double  : slot energies after the sweeps of each step */
 };
 
 orc_trace* orc_trace_new(void) {
@@ -773,12 +773,12 @@ int orc_solve(orc_problem* p, const orc_params* prm, orc_result* res,
                 if (trace) { trace->u.n += used; uint64_t o = trace->u.n; vpush(&trace->off, &o); }
             }
         }
+        if (trace) for (uint64_t k = 0; k < R; k++) vpush(&trace->energy, &w->Eg[w->bidx[k]]);
         for (uint64_t m = 0; m + 1 < Nt; m++) { try_exchange(w, 0); try_exchange(w, 1); }
         if (prm->icm) {
             for (int64_t k = (int64_t)Nt - 1; k >= (int64_t)Nt - (int64_t)Nc; k--)
                 if (icm_step(w, (uint64_t)k, t1, t2, tmp, added)) { rc = -3; break; }
         }
-        if (trace) for (uint64_t r = 0; r < R; r++) vpush(&trace->energy, &w->E[r]);
     }
     /* gather_best_energy_values (src/mpi_utils.cc:103-163), one rank */
     double best = DBL_MAX;

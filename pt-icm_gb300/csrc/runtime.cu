@@ -929,6 +929,38 @@ int pticm_get_profile(pticm_ctx* c, double* mean_ms, double* max_ms) {
     return PTICM_OK;
 }
 
+int pticm_enable_energy_histograms(pticm_ctx* c, uint64_t from_step) {
+    if (!c) return fail(PTICM_ERR_INVALID, "null argument");
+    // every energy lies in [-W, W], W = sum |J| over edges + sum |h|, and has
+    // the parity of W: bins of width 2 from -W are exact energy levels
+    const HostProblem& P = c->P;
+    long long directed = 0, lin = 0;
+    for (int64_t i = 0; i < P.n; i++) {
+        lin += std::llabs((long long)P.h[i]);
+        for (int64_t a = P.row[i]; a < P.row[i + 1]; a++) directed += std::llabs((long long)P.w[a]);
+    }
+    const long long wabs = directed / 2 + lin;
+    if ((unsigned long long)(wabs + 1) * (unsigned long long)c->R > (1ull << 31))
+        return fail(PTICM_ERR_UNSUPPORTED, "energy range too large for per-slot histograms");
+    c->hist_lo = -wabs;
+    c->hist_nbins = wabs + 1;
+    c->hist_from = from_step;
+    CK(c->d_hist.alloc((size_t)c->R * (size_t)c->hist_nbins));
+    return PTICM_OK;
+}
+
+int pticm_get_energy_histograms(pticm_ctx* c, uint32_t* hist, int64_t* e_lo, uint64_t* nbins) {
+    if (!c) return fail(PTICM_ERR_INVALID, "null argument");
+    if (!c->d_hist.p) return fail(PTICM_ERR_INVALID, "energy histograms are not enabled");
+    if (e_lo) *e_lo = c->hist_lo;
+    if (nbins) *nbins = (uint64_t)c->hist_nbins;
+    if (hist) {
+        CK(cudaStreamSynchronize(c->stream));
+        CK(cudaMemcpy(hist, c->d_hist.p, c->d_hist.n * sizeof(unsigned), cudaMemcpyDeviceToHost));
+    }
+    return PTICM_OK;
+}
+
 int pticm_mhist_dos(const uint32_t* hist, const uint64_t* hist_off, const uint64_t* hist_len, uint32_t nt,
                     const double* beta_hist, const double* emin, double estep, uint64_t n, double max_emax,
                     double* logdos, uint64_t logdos_cap, double* logZ, uint64_t* nbins, uint64_t* iterations) {
@@ -981,19 +1013,8 @@ int pticm_cae_ladder(const pticm_problem* p, uint64_t seed, double T0, double T1
     if (int rc = pticm_create(p, &o, &c)) return rc;
     std::unique_ptr<pticm_ctx> hold(c);
     if (int rc = pticm_set_ladder(c, hb.data(), nt, 0)) return rc;
-    // every energy lies in [-W, W], W = sum |J| over edges + sum |h|, and has
-    // the parity of W: bins of width 2 from -W are exact energy levels
-    long long directed = 0, lin = 0;
-    for (int64_t i = 0; i < P.n; i++) {
-        lin += std::llabs((long long)P.h[i]);
-        for (int64_t a = P.row[i]; a < P.row[i + 1]; a++) directed += std::llabs((long long)P.w[a]);
-    }
-    const long long wabs = directed / 2 + lin;
-    c->hist_lo = -wabs;
-    c->hist_nbins = wabs + 1;
-    c->hist_from = burn_in;
-    CK(c->d_hist.alloc((size_t)nt * (size_t)c->hist_nbins));
     if (int rc = pticm_init_states(c, seed)) return rc;
+    if (int rc = pticm_enable_energy_histograms(c, burn_in)) return rc;
     if (int rc = pticm_run(c, burn_in + samples, 7)) return rc;
     std::vector<unsigned> habs;
     CK(c->d_hist.download(habs));

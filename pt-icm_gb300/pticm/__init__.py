@@ -87,6 +87,8 @@ def lib():
         "pticm_philox_probe": [P, P, P, C.c_int],
         "pticm_set_profiling": [P, C.c_int],
         "pticm_cae_ladder": [P, u64, dbl, dbl, C.c_int, u32, dbl, dbl, dbl, u64, u64, P, P],
+        "pticm_enable_energy_histograms": [P, u64],
+        "pticm_get_energy_histograms": [P, P, P, P],
         "pticm_mhist_dos": [P, P, P, u32, P, P, dbl, u64, dbl, P, u64, P, P, P],
         "pticm_cae_walk": [P, u64, dbl, dbl, dbl, dbl, dbl, dbl, u32, P, P],
         "pticm_get_profile": [P, P, P],
@@ -298,6 +300,18 @@ class Context:
         names = ("sweep", "barrier", "exchange", "icm", "total", "icm_diff", "icm_seed", "icm_union",
                  "icm_flip", "icm_energy", "x_draw", "x_levels", "x_apply", "x_shuffle")
         return dict(zip(names, mean)), dict(zip(names, mx))
+
+    def enable_energy_histograms(self, from_step=0):
+        _check(lib().pticm_enable_energy_histograms(self._h, from_step))
+
+    def energy_histograms(self):
+        """(histograms [R, nbins], energies of the bins [nbins])."""
+        lo = C.c_int64()
+        nb = C.c_uint64()
+        _check(lib().pticm_get_energy_histograms(self._h, None, C.byref(lo), C.byref(nb)))
+        h = np.zeros((self.R, nb.value), np.uint32)
+        _check(lib().pticm_get_energy_histograms(self._h, _p(h), C.byref(lo), C.byref(nb)))
+        return h, lo.value + 2 * np.arange(nb.value)
 
     def verify(self) -> int:
         mm = C.c_uint64()

@@ -1,0 +1,56 @@
+"""The pt_icm command line (src/main.cc) on the GPU engine: the reference's
+flags, the reference's report keys, internally consistent values."""
+import os
+import re
+import subprocess
+
+import pytest
+
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CLI = os.path.join(ROOT, "pt-icm_gb300", "bin", "pt_icm")
+G = os.path.join(ROOT, "tests", "golden", "graphs")
+
+
+def _run(*args):
+    out = subprocess.run([CLI, *args], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    return out.stdout
+
+
+def _parse(text):
+    rep = {}
+    for line in text.splitlines():
+        m = re.match(r"^(\w+): (.*)$", line.strip())
+        if m:
+            rep[m.group(1)] = m.group(2).strip()
+    return rep
+
+
+@pytest.mark.parametrize("flag", ["-p", "-g"])
+def test_cli_report(flag):
+    path = os.path.join(G, "pmL10.gset")
+    rep = _parse(_run(flag, path, "-s", "3", "-r", "8", "--pts", "500", "--icm", "-T0", "0.5", "-T1", "3.0"))
+    for key in ("swap_rates", "swap_attempts", "swap_successes", "best_state_energy", "best_state_sweep",
+                "best_energy", "best_maxcut", "num_of_flips", "num_of_swaps", "best_state", "Total time"):
+        assert key in rep, key
+    att = [int(x) for x in rep["swap_attempts"][1:-1].split(",")]
+    suc = [int(x) for x in rep["swap_successes"][1:-1].split(",")]
+    assert len(att) == 16 and sum(suc) == int(rep["num_of_swaps"])
+    assert float(rep["best_state_energy"]) == float(rep["best_energy"])
+    # the ground state of this +-J lattice, as the reference finds it
+    best_ref = min(O.solve(O.Problem.load(path, s), seed=s, Nt=8, pts=400, icm=True, T0=0.5, T1=3.0)["best_energy"]
+                   for s in (1, 2))
+    assert float(rep["best_energy"]) == best_ref
+
+
+def test_cli_preprocess_ladder():
+    path = os.path.join(G, "pmL10.gset")
+    text = _run("-p", path, "-s", "4", "-r", "10", "--pts", "200", "--preprocess", "--preprocess-samples", "500")
+    lines = [l for l in text.splitlines() if l.startswith("[")]
+    ladder = [float(x) for x in lines[-1][1:-1].split(",")]
+    assert ladder[0] == pytest.approx(1 / 0.6, rel=1e-6)
+    assert all(a > b for a, b in zip(ladder, ladder[1:]))

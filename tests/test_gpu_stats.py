@@ -1,0 +1,90 @@
+"""Statistical parity of production mode with the reference's algorithm.
+
+The GPU engine and the C oracle (the reference's arithmetic and random
+stream) run independent seeds of the same problem and ladder.  Per
+temperature, the mean energy after burn-in and the exchange acceptance of
+each neighbouring pair must agree within 3 sigma of their seed-to-seed
+spread (at most one of all comparisons beyond 3 sigma, none beyond 4.5).
+Both production exchange orders are checked.  On small instances the best
+energy found must equal the oracle's best.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+G = os.path.join(os.path.dirname(__file__), "golden", "graphs")
+SEEDS = 8
+BURN = 300
+
+
+def _oracle_runs(path, nt, T0, T1, pts, icm):
+    means, rates = [], []
+    for s in range(SEEDS):
+        o = O.solve(O.Problem.load(path, 100 + s), seed=100 + s, Nt=nt, pts=pts, icm=icm, T0=T0, T1=T1, trace=True)
+        se = o["trace"]["step_energy"]          # [pts, 2nt] slot energies after the sweeps
+        means.append(se[BURN:].reshape(-1, 2, nt).mean(axis=(0, 1)))
+        att = o["swap_attempts"].astype(float)
+        suc = o["swap_successes"].astype(float)
+        rates.append((suc[:nt - 1] + suc[nt:2 * nt - 1]) / np.maximum(att[:nt - 1] + att[nt:2 * nt - 1], 1))
+    return np.array(means), np.array(rates)
+
+
+def _gpu_runs(path, nt, T0, T1, pts, icm, exchange):
+    import pticm
+    prob = pticm.Problem.load(path)
+    beta = pticm.beta_linspace(T0, T1, nt)
+    means, rates = [], []
+    for s in range(SEEDS):
+        ctx = pticm.Context(prob, nt=nt, seed=500 + s, icm=icm, exchange=exchange)
+        ctx.set_ladder(beta)
+        ctx.init_states(500 + s)
+        ctx.enable_energy_histograms(BURN)
+        ctx.run(pts)
+        h, e = ctx.energy_histograms()
+        m = (h * e[None, :]).sum(axis=1) / h.sum(axis=1)
+        means.append(m.reshape(2, nt).mean(axis=0))
+        _, att, suc = ctx.stats()
+        att = att.astype(float)
+        suc = suc.astype(float)
+        rates.append((suc[:nt - 1] + suc[nt:2 * nt - 1]) / np.maximum(att[:nt - 1] + att[nt:2 * nt - 1], 1))
+    return np.array(means), np.array(rates)
+
+
+def _agree(a, b):
+    diff = a.mean(axis=0) - b.mean(axis=0)
+    sig = np.sqrt(a.var(axis=0, ddof=1) / len(a) + b.var(axis=0, ddof=1) / len(b)) + 1e-12
+    z = np.abs(diff) / sig
+    return z
+
+
+@pytest.mark.parametrize("exchange", [1, 0])
+@pytest.mark.parametrize("g,nt,T0,T1,icm", [("pmL10.gset", 8, 0.5, 3.0, True), ("rnd60_pm", 8, 0.5, 3.0, True),
+                                             ("rnd200_w1", 10, 0.5, 15.0, False)])
+def test_energy_and_acceptance_match_reference_algorithm(g, nt, T0, T1, icm, exchange):
+    path = os.path.join(G, g)
+    pts = 1500
+    om, orate = _oracle_runs(path, nt, T0, T1, pts, icm)
+    gm, grate = _gpu_runs(path, nt, T0, T1, pts, icm, exchange)
+    z = np.concatenate([_agree(gm, om), _agree(grate, orate)])
+    assert (z > 3.0).sum() <= 1, z
+    assert z.max() < 4.5, z
+
+
+@pytest.mark.parametrize("g,nt,T0,T1", [("pmL10.gset", 8, 0.5, 3.0), ("rnd60_pm", 8, 0.5, 3.0),
+                                         ("rnd200_w1", 12, 0.5, 15.0), ("lin40.ising", 8, 0.5, 3.0),
+                                         ("ferroL12.gset", 10, 0.5, 3.5)])
+def test_best_energy_matches_reference_on_small_instances(g, nt, T0, T1):
+    import pticm
+    path = os.path.join(G, g)
+    best_ref = min(O.solve(O.Problem.load(path, s), seed=s, Nt=nt, pts=600, icm=True, T0=T0, T1=T1)["best_energy"]
+                   for s in range(1, 4))
+    prob = pticm.Problem.load(path)
+    out = pticm.solve(prob, seed=11, Nt=nt, pts=3000, T0=T0, T1=T1, icm=True)
+    assert out["best_energy"] == best_ref
+    E, cut = prob.evaluate(out["best_state"][None, :])
+    assert E[0] == out["best_energy"]

@@ -24,6 +24,13 @@
 #include <stddef.h>
 #include <stdint.h>
 
+/* The library is built with hidden visibility; only this C ABI is exported. */
+#if defined(__GNUC__)
+#define PTICM_API __attribute__((visibility("default")))
+#else
+#define PTICM_API
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -61,25 +68,25 @@ typedef struct pticm_problem_info {
  * vertices, else 1-based; a missing weight is 1; ".ising" files carry a
  * linear-term block.  Couplings and linear terms must be integers in
  * [-127, 127] (PTICM_ERR_UNSUPPORTED otherwise). */
-int pticm_problem_load_gset(const char* path, pticm_problem** out);
+PTICM_API int pticm_problem_load_gset(const char* path, pticm_problem** out);
 
 /* Problem(weights, src, dest, linear, seed, burn_in, N, M)
  * include/problem.hh:43-62.  `h` may be NULL. */
-int pticm_problem_from_coo(int64_t n, int64_t m, const int32_t* src, const int32_t* dst,
+PTICM_API int pticm_problem_from_coo(int64_t n, int64_t m, const int32_t* src, const int32_t* dst,
                            const double* w, const double* h, pticm_problem** out);
 
 /* Problem(formulation, linear, seed, burn_in, N)  include/problem.hh:23-42:
  * a dense row-major n*n coupling matrix (only j != i entries are used; zero
  * entries are not edges).  `h` may be NULL. */
-int pticm_problem_from_dense(int64_t n, const double* J, const double* h, pticm_problem** out);
+PTICM_API int pticm_problem_from_dense(int64_t n, const double* J, const double* h, pticm_problem** out);
 
-void pticm_problem_free(pticm_problem* p);
-int pticm_problem_get_info(const pticm_problem* p, pticm_problem_info* out);
+PTICM_API void pticm_problem_free(pticm_problem* p);
+PTICM_API int pticm_problem_get_info(const pticm_problem* p, pticm_problem_info* out);
 
 /* Problem::energy, Problem::maxcut, Problem::calculate_dE
  * src/problem.cc:33-162, computed on the GPU for `count` states
  * (count*n bytes).  `dE` (count*n doubles) may be NULL. */
-int pticm_problem_evaluate(const pticm_problem* p, int64_t count, const uint8_t* states,
+PTICM_API int pticm_problem_evaluate(const pticm_problem* p, int64_t count, const uint8_t* states,
                            double* energy, double* maxcut, double* dE);
 
 /* --------------------------------------------------------- PT contexts -- */
@@ -99,28 +106,28 @@ typedef struct pticm_opts {
                             /* 2 union-find, 3 label propagation              */
 } pticm_opts;
 
-void pticm_opts_default(pticm_opts* o);
+PTICM_API void pticm_opts_default(pticm_opts* o);
 
 /* State of solve() between initialisation and reporting
  * (src/solver.cc:16-166, include/mpi_defs.hh:33-65): all replicas of the
  * problem resident on the current CUDA device. */
-int pticm_create(const pticm_problem* p, const pticm_opts* o, pticm_ctx** out);
-void pticm_destroy(pticm_ctx* c);
+PTICM_API int pticm_create(const pticm_problem* p, const pticm_opts* o, pticm_ctx** out);
+PTICM_API void pticm_destroy(pticm_ctx* c);
 
 /* initialize_temperatures (src/initialization.cc:103-191) with an explicit
  * ladder of nt inverse temperatures (slot k of every chain gets beta[k]).
  * The ICM pair count follows src/initialization.cc:158-164 (entries from the
  * top slot down while beta >= char_scale) unless `nc` >= 0 sets it. */
-int pticm_set_ladder(pticm_ctx* c, const double* beta, uint32_t nt, int32_t nc);
+PTICM_API int pticm_set_ladder(pticm_ctx* c, const double* beta, uint32_t nt, int32_t nc);
 
 /* beta_linspace (src/mpi_utils.cc:6-22), linear in beta, same FP64 steps. */
-int pticm_beta_linspace(double* beta, double T0, double T1, uint64_t nt, int inverse);
+PTICM_API int pticm_beta_linspace(double* beta, double T0, double T1, uint64_t nt, int inverse);
 
 /* initialize_replicas (src/initialization.cc:63-76): Bernoulli(1/2) spins
  * from a counter-based stream, then a from-scratch field/energy pass. */
-int pticm_init_states(pticm_ctx* c, uint64_t seed);
+PTICM_API int pticm_init_states(pticm_ctx* c, uint64_t seed);
 /* Explicit initial spins: R*n bytes (0/1), replica r = chain*nt + k. */
-int pticm_set_states(pticm_ctx* c, const uint8_t* states);
+PTICM_API int pticm_set_states(pticm_ctx* c, const uint8_t* states);
 
 #define PTICM_PHASE_SWEEP 1u
 #define PTICM_PHASE_EXCHANGE 2u
@@ -130,7 +137,7 @@ int pticm_set_states(pticm_ctx* c, const uint8_t* states);
 /* The PT loop (src/solver.cc:67-127): `pt_steps` steps of sweeps, exchange
  * and ICM. `phase_mask` selects phases (1 sweep, 2 exchange, 4 ICM; 7 = all)
  * so that each phase can be checked on its own. */
-int pticm_run(pticm_ctx* c, uint64_t pt_steps, uint32_t phase_mask);
+PTICM_API int pticm_run(pticm_ctx* c, uint64_t pt_steps, uint32_t phase_mask);
 
 typedef struct pticm_stats {
     uint64_t pt_steps;      /* steps run so far                               */
@@ -143,24 +150,24 @@ typedef struct pticm_stats {
 
 /* swap_attempts / swap_successes per slot (2*nt entries for two chains, as
  * printed by src/solver.cc:152-153); either array may be NULL. */
-int pticm_get_stats(pticm_ctx* c, pticm_stats* s, uint64_t* swap_attempts, uint64_t* swap_successes);
+PTICM_API int pticm_get_stats(pticm_ctx* c, pticm_stats* s, uint64_t* swap_attempts, uint64_t* swap_successes);
 
 /* gather_best_energy_values (src/mpi_utils.cc:103-163): lowest energy seen
  * by any replica, the replica's sweep counter then, and that state (n bytes). */
-int pticm_get_best(pticm_ctx* c, double* energy, uint64_t* sweep, uint8_t* state, int64_t* replica);
+PTICM_API int pticm_get_best(pticm_ctx* c, double* energy, uint64_t* sweep, uint8_t* state, int64_t* replica);
 
 /* Current replicas: states (R*n bytes), energies (R), local fields
  * f_i = sum_j J_ij s_j (R*n, original site order) and the temperature slot
  * of each replica.  Any pointer may be NULL. */
-int pticm_get_replicas(pticm_ctx* c, uint8_t* states, int64_t* energy, int32_t* fields, uint32_t* slot_of_replica);
+PTICM_API int pticm_get_replicas(pticm_ctx* c, uint8_t* states, int64_t* energy, int32_t* fields, uint32_t* slot_of_replica);
 
 /* Ladder and slot -> replica map (beta_indices of src/replica_exchange.cc). */
-int pticm_get_ladder(pticm_ctx* c, double* beta, uint32_t* slot_to_replica, uint32_t* nc);
+PTICM_API int pticm_get_ladder(pticm_ctx* c, double* beta, uint32_t* slot_to_replica, uint32_t* nc);
 
 /* From-scratch recompute of every replica's fields and energy on the GPU,
  * compared with the incrementally tracked values; `mismatches` counts
  * differing sites and energies (0 = bit-exact). */
-int pticm_verify(pticm_ctx* c, uint64_t* mismatches);
+PTICM_API int pticm_verify(pticm_ctx* c, uint64_t* mismatches);
 
 /* Phase timers (tracing): when enabled, every block of the following
  * pticm_run calls accumulates clock64 cycles spent in the sweep, the
@@ -171,18 +178,18 @@ int pticm_verify(pticm_ctx* c, uint64_t* mismatches);
  * milliseconds at the device's maximum SM clock and reports the mean and
  * the maximum over blocks; enabling again clears the counters. */
 #define PTICM_PROFILE_SLOTS 14
-int pticm_set_profiling(pticm_ctx* c, int enable);
-int pticm_get_profile(pticm_ctx* c, double* mean_ms, double* max_ms);
+PTICM_API int pticm_set_profiling(pticm_ctx* c, int enable);
+PTICM_API int pticm_get_profile(pticm_ctx* c, double* mean_ms, double* max_ms);
 
 /* Per-temperature energy histograms (the observables the reference's --log
  * path was to log, src/main.cc:490-530, and the multihistogram input): from PT
  * step `from_step` on, every step adds the energy of the replica at each slot
  * after its sweeps, in exact levels E = e_lo + 2*bin (every energy has the
  * parity of e_lo).  Enabling clears the counts. */
-int pticm_enable_energy_histograms(pticm_ctx* c, uint64_t from_step);
+PTICM_API int pticm_enable_energy_histograms(pticm_ctx* c, uint64_t from_step);
 /* Rows of slot k at hist[k*nbins ...] (R rows); pass hist = NULL to query
  * nbins and e_lo first. */
-int pticm_get_energy_histograms(pticm_ctx* c, uint32_t* hist, int64_t* e_lo, uint64_t* nbins);
+PTICM_API int pticm_get_energy_histograms(pticm_ctx* c, uint32_t* hist, int64_t* e_lo, uint64_t* nbins);
 
 /* -------------------------------------------- multihistogram ladder -- */
 /* get_beta (src/cae_estimator.cc:295-428) on the GPU: a pilot PT run
@@ -194,7 +201,7 @@ int pticm_get_energy_histograms(pticm_ctx* c, uint32_t* hist, int64_t* e_lo, uin
  * beta_out (>= nt entries) receives the descending ladder, *count its length.
  * The reference calls it with estep 2 and r 0.4 (src/initialization.cc:110)
  * and a burn-in of 5000 (src/cae_estimator.cc:74). */
-int pticm_cae_ladder(const pticm_problem* p, uint64_t seed, double T0, double T1, int inverse, uint32_t nt,
+PTICM_API int pticm_cae_ladder(const pticm_problem* p, uint64_t seed, double T0, double T1, int inverse, uint32_t nt,
                      double estep, double step_size, double r, uint64_t samples, uint64_t burn_in,
                      double* beta_out, uint32_t* count);
 
@@ -205,13 +212,13 @@ int pticm_cae_ladder(const pticm_problem* p, uint64_t seed, double T0, double T1
  * nbins = ceil((max_emax - min_j emin[j]) / estep) values of ln g (up to
  * logdos_cap) and the nt values of ln Z; iterates until
  * sum_j ((lnZ_j - lnZ'_j) / lnZ'_j)^2 <= 1e-7. */
-int pticm_mhist_dos(const uint32_t* hist, const uint64_t* hist_off, const uint64_t* hist_len, uint32_t nt,
+PTICM_API int pticm_mhist_dos(const uint32_t* hist, const uint64_t* hist_off, const uint64_t* hist_len, uint32_t nt,
                     const double* beta_hist, const double* emin, double estep, uint64_t n, double max_emax,
                     double* logdos, uint64_t logdos_cap, double* logZ, uint64_t* nbins, uint64_t* iterations);
 
 /* The constant-acceptance walk alone (src/cae_estimator.cc:367-425) from a
  * density of states; host code (no GPU needed), O(nbins) per candidate. */
-int pticm_cae_walk(const double* logdos, uint64_t nbins, double min_emin, double estep, double beta_start,
+PTICM_API int pticm_cae_walk(const double* logdos, uint64_t nbins, double min_emin, double estep, double beta_start,
                    double beta_end, double step_size, double r, uint32_t num_temps, double* beta_out,
                    uint32_t* count);
 
@@ -232,7 +239,7 @@ typedef struct pticm_trace {
     const int64_t* icm_seed;       /* pt_steps*nc seeds, original index or -1   */
 } pticm_trace;
 
-int pticm_replay(pticm_ctx* c, const pticm_trace* t);
+PTICM_API int pticm_replay(pticm_ctx* c, const pticm_trace* t);
 
 /* ----------------------------------------------- no device allocation -- */
 /* For callers that cannot call cudaMalloc (their host framework owns every
@@ -269,14 +276,14 @@ typedef struct pticm_noalloc_io {
     uint8_t* best_states_out;    /* device, R*n: the matching states, or NULL    */
 } pticm_noalloc_io;
 
-int pticm_run_noalloc(const pticm_problem* p, const pticm_opts* o, const double* beta, uint32_t nt, int32_t nc,
+PTICM_API int pticm_run_noalloc(const pticm_problem* p, const pticm_opts* o, const double* beta, uint32_t nt, int32_t nc,
                       const pticm_noalloc_io* io, uint64_t step0, uint64_t pt_steps, void* stream);
 
 /* ----------------------------------------------------------- utilities -- */
-const char* pticm_last_error(void);
-const char* pticm_version(void);
+PTICM_API const char* pticm_last_error(void);
+PTICM_API const char* pticm_version(void);
 /* Philox4x32-10 known-answer probe: out[4*i..] = philox(ctr[4*i..], key[2*i..]). */
-int pticm_philox_probe(const uint32_t* ctr, const uint32_t* key, uint32_t* out, int count);
+PTICM_API int pticm_philox_probe(const uint32_t* ctr, const uint32_t* key, uint32_t* out, int count);
 
 #ifdef __cplusplus
 }

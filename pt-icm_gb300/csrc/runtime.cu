@@ -992,7 +992,6 @@ int pticm_cae_ladder(const pticm_problem* p, uint64_t seed, double T0, double T1
     if (!p || !beta_out || !count || nt < 2 || samples == 0 || !(estep > 0))
         return fail(PTICM_ERR_INVALID, "invalid arguments");
     if (int rc = check_device()) return rc;
-    const HostProblem& P = p->hp;
     // histogram temperatures: linear in beta from the largest beta down
     // (src/cae_estimator.cc:308-328)
     double beta_start = inverse ? T0 : 1 / T0, beta_end = inverse ? T1 : 1 / T1;

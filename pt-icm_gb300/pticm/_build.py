@@ -21,7 +21,7 @@ LIB = os.path.join(PKG, "libpticm_gb300.so")
 CLI = os.path.join(ROOT, "bin", "pt_icm")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
+NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",
            "--expt-relaxed-constexpr"] + ARCH
 INCS = ["-I", os.path.join(REPO, "include"), "-I", CSRC]
 

@@ -33,9 +33,11 @@ def _parse(text):
 @pytest.mark.parametrize("flag", ["-p", "-g"])
 def test_cli_report(flag):
     path = os.path.join(G, "pmL10.gset")
-    rep = _parse(_run(flag, path, "-s", "3", "-r", "8", "--pts", "500", "--icm", "-T0", "0.5", "-T1", "3.0"))
+    text = _run(flag, path, "-s", "3", "-r", "8", "--pts", "500", "--icm", "-T0", "0.5", "-T1", "3.0")
+    assert re.search(r"^Total time: [0-9.]+$", text, re.M)
+    rep = _parse(text)
     for key in ("swap_rates", "swap_attempts", "swap_successes", "best_state_energy", "best_state_sweep",
-                "best_energy", "best_maxcut", "num_of_flips", "num_of_swaps", "best_state", "Total time"):
+                "best_energy", "best_maxcut", "num_of_flips", "num_of_swaps", "best_state"):
         assert key in rep, key
     att = [int(x) for x in rep["swap_attempts"][1:-1].split(",")]
     suc = [int(x) for x in rep["swap_successes"][1:-1].split(",")]

@@ -18,8 +18,8 @@ from oracle import pyoracle as O
 pytestmark = pytest.mark.gpu
 
 G = os.path.join(os.path.dirname(__file__), "golden", "graphs")
-SEEDS = 8
-BURN = 300
+SEEDS = 12
+BURN = 800
 
 
 def _oracle_runs(path, nt, T0, T1, pts, icm):
@@ -67,7 +67,7 @@ def _agree(a, b):
                                              ("rnd200_w1", 10, 0.5, 15.0, False)])
 def test_energy_and_acceptance_match_reference_algorithm(g, nt, T0, T1, icm, exchange):
     path = os.path.join(G, g)
-    pts = 1500
+    pts = 3000
     om, orate = _oracle_runs(path, nt, T0, T1, pts, icm)
     gm, grate = _gpu_runs(path, nt, T0, T1, pts, icm, exchange)
     z = np.concatenate([_agree(gm, om), _agree(grate, orate)])

@@ -279,6 +279,38 @@ typedef struct pticm_noalloc_io {
 PTICM_API int pticm_run_noalloc(const pticm_problem* p, const pticm_opts* o, const double* beta, uint32_t nt, int32_t nc,
                       const pticm_noalloc_io* io, uint64_t step0, uint64_t pt_steps, void* stream);
 
+/* --------------------------------------------------- tensor-core GEMM -- */
+/* C[M x N] = act(A[M x K] . B[N x K]^T + bias) on the tcgen05 tensor cores
+ * (BF16 operands given as raw uint16 bit patterns, K-major; FP32 result;
+ * act 0 = none, 1 = SiLU; K a multiple of 64).  Host buffers; used to check
+ * the surrogate network's GEMM against a reference. */
+PTICM_API int pticm_tc_gemm_check(int M, int N, int K, const uint16_t* A, const uint16_t* B, const float* bias,
+                                  int act, float* C);
+
+/* ------------------------------------------- surrogate ln g(E) network -- */
+/* A multilayer perceptron f(features, e) -> ln g / N: 7 inputs, four hidden
+ * layers of 256 SiLU units, one linear output; BF16 weights and activations
+ * with FP32 accumulation on the tcgen05 tensor cores, FP32 master weights
+ * trained with Adam.  Parameters are one flat FP32 vector of
+ * pticm_mlp_param_count() values: W1 [256 x 64] (input columns 7.. unused),
+ * b1, W2 [256 x 256], b2, W3, b3, W4, b4, w5 [256], b5.  No counterpart in
+ * the reference (the benchmark spec's learned ladder). */
+typedef struct pticm_mlp pticm_mlp;
+PTICM_API int pticm_mlp_create(uint64_t seed, uint32_t batch, pticm_mlp** out);
+PTICM_API void pticm_mlp_destroy(pticm_mlp* m);
+PTICM_API uint64_t pticm_mlp_param_count(void);
+PTICM_API int pticm_mlp_get_params(pticm_mlp* m, float* out);
+PTICM_API int pticm_mlp_set_params(pticm_mlp* m, const float* in);
+/* Stage n training rows: x (n x 7) and y (n). */
+PTICM_API int pticm_mlp_set_data(pticm_mlp* m, const float* x, const float* y, uint64_t n);
+/* Mean squared error and its gradient (flat, FP32) on n <= batch rows. */
+PTICM_API int pticm_mlp_gradients(pticm_mlp* m, const float* x, const float* y, uint32_t n, float* grads,
+                                  float* loss);
+/* `steps` Adam steps on shuffled mini-batches; loss_per_step may be NULL. */
+PTICM_API int pticm_mlp_train(pticm_mlp* m, const float* x, const float* y, uint64_t n, uint32_t steps, float lr,
+                              uint64_t seed, float* loss_per_step);
+PTICM_API int pticm_mlp_predict(pticm_mlp* m, const float* x, uint64_t n, float* y);
+
 /* ----------------------------------------------------------- utilities -- */
 PTICM_API const char* pticm_last_error(void);
 PTICM_API const char* pticm_version(void);

@@ -1,0 +1,183 @@
+// tc_gemm.cu -- BF16 GEMM on the 5th-generation tensor cores (tcgen05, sm_103a)
+// for the surrogate-ladder MLP.
+//
+//   C[M x N] = act(A[M x K] . B[N x K]^T + bias[N])      (A, B bf16, K-major)
+//
+// One CTA of 128 threads computes a 128 x 128 tile.  Operand tiles of
+// 128 x 64 are staged in shared memory in the canonical K-major layout
+// without swizzle: 8-row x 16-byte core matrices, K-adjacent core matrices
+// 128 B apart (leading byte offset), 8-row groups 1024 B apart (stride byte
+// offset).  Thread 0 issues tcgen05.mma.kind::f16 (M=128, N=128, K=16 each,
+// FP32 accumulation) into a tensor-memory accumulator and commits to an
+// mbarrier; the four warps then read their 32 accumulator lanes with
+// tcgen05.ld and apply the epilogue (bias, optional SiLU, FP32 and/or BF16
+// stores).  Every wait is bounded; a timeout is recorded in a status word.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "pticm_device.cuh"
+
+namespace pticm {
+
+constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 64;
+constexpr uint32_t TC_TILE_BYTES = TC_BM * TC_BK * 2;   // 16 KB per operand tile
+constexpr uint32_t TC_TMEM_COLS = 256;                   // allocation (128 used)
+
+enum TcAct : int { TC_ACT_NONE = 0, TC_ACT_SILU = 1 };
+
+// Shared-memory matrix descriptor: start address, leading (K) and stride
+// (M/N) byte offsets in 16-byte units, descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t tc_smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t tc_idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Copy one 128 x 64 bf16 tile (rows r0.., columns k0..) of a K-major matrix
+// into the core-matrix layout; thread t moves row t.
+__device__ __forceinline__ void tc_stage_tile(uint8_t* dst, const __nv_bfloat16* src, long long ld, int r0, int k0,
+                                              int rows) {
+    const int m = threadIdx.x;
+    uint4 v[8];
+    if (r0 + m < rows) {
+        const uint4* p = reinterpret_cast<const uint4*>(src + (long long)(r0 + m) * ld + k0);
+#pragma unroll
+        for (int c = 0; c < 8; c++) v[c] = p[c];
+    } else {
+#pragma unroll
+        for (int c = 0; c < 8; c++) v[c] = make_uint4(0, 0, 0, 0);
+    }
+    uint8_t* base = dst + (m >> 3) * 1024 + (m & 7) * 16;
+#pragma unroll
+    for (int c = 0; c < 8; c++) *reinterpret_cast<uint4*>(base + c * 128) = v[c];
+}
+
+__global__ void __launch_bounds__(128, 1)
+tc_gemm_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restrict__ B, int M, int N, int K,
+               const float* __restrict__ bias, int act, float* __restrict__ Cf, __nv_bfloat16* __restrict__ Cb,
+               long long ldc, DevStatus* status, int* abort_flag) {
+    extern __shared__ __align__(1024) uint8_t tc_smem[];
+    uint8_t* sA = tc_smem;
+    uint8_t* sB = tc_smem + TC_TILE_BYTES;
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tmem_base_s;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.x * TC_BM, n0 = blockIdx.y * TC_BN;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
+                     "r"(TC_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (threadIdx.x == 0) mbar_init(&mbar, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base_s;
+
+    const uint32_t idesc = tc_idesc_bf16(TC_BM, TC_BN);
+    const uint32_t aaddr = smem_u32(sA), baddr = smem_u32(sB);
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int k0 = 0; k0 < K; k0 += TC_BK) {
+        tc_stage_tile(sA, A, K, m0, k0, M);
+        tc_stage_tile(sB, B, K, n0, k0, N);
+        tc_fence_proxy_async();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+            for (int kk = 0; kk < TC_BK / 16; kk++) {
+                const uint64_t da = tc_smem_desc(aaddr + kk * 256, 128, 1024);
+                const uint64_t db = tc_smem_desc(baddr + kk * 256, 128, 1024);
+                const uint32_t accumulate = (k0 > 0 || kk > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\t"
+                    "setp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+                    "l"(da), "l"(db), "r"(idesc), "r"(accumulate)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_u32(&mbar))
+                         : "memory");
+        }
+        // the tiles may be overwritten only after the MMAs have read them
+        if (!mbar_wait_bounded(&mbar, phase)) ok = false;
+        phase ^= 1u;
+        if (!ok) break;
+    }
+    if (!ok) {
+        // record the failure, then give the MMAs in flight one more bounded
+        // wait before the accumulator is released
+        if (threadIdx.x == 0 && status) dev_fail(status, abort_flag, DEV_TMA_TIMEOUT, 100, blockIdx.x, blockIdx.y);
+        mbar_wait_bounded(&mbar, phase ^ 1u);
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+    // epilogue: warp w owns accumulator lanes (rows) 32w .. 32w+31
+    const int row = m0 + warp * 32 + lane;
+    if (ok) {
+#pragma unroll 1
+        for (int c0 = 0; c0 < TC_BN; c0 += 32) {
+            uint32_t r[32];
+            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                  "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+                  "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (row < M) {
+#pragma unroll
+                for (int j = 0; j < 32; j++) {
+                    const int col = n0 + c0 + j;
+                    if (col >= N) continue;
+                    float v = __uint_as_float(r[j]) + (bias ? bias[col] : 0.0f);
+                    if (Cf) Cf[(long long)row * ldc + col] = v;
+                    if (act == TC_ACT_SILU) v = v / (1.0f + __expf(-v));
+                    if (Cb) Cb[(long long)row * ldc + col] = __float2bfloat16_rn(v);
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+}
+
+// Launch: M, N multiples of 128 not required (rows/cols beyond are masked),
+// K a multiple of 64 and both operands 16-byte aligned with row stride K.
+cudaError_t tc_gemm(const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N, int K, const float* bias, int act,
+                    float* Cf, __nv_bfloat16* Cb, long long ldc, DevStatus* status, int* abort_flag,
+                    cudaStream_t st) {
+    const size_t smem = 2 * TC_TILE_BYTES + 1024;
+    cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((M + TC_BM - 1) / TC_BM, (N + TC_BN - 1) / TC_BN);
+    tc_gemm_kernel<<<grid, 128, smem, st>>>(A, B, M, N, K, bias, act, Cf, Cb, ldc, status, abort_flag);
+    return cudaGetLastError();
+}
+
+}  // namespace pticm

@@ -1,0 +1,38 @@
+"""The tcgen05 BF16 GEMM against a plain PyTorch FP32 reference of the same
+op (bf16 operands, fp32 accumulation)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _bf16_bits(x):
+    import torch
+    t = torch.from_numpy(np.ascontiguousarray(x, np.float32)).to(torch.bfloat16)
+    return t.view(torch.int16).numpy().view(np.uint16), t.to(torch.float32)
+
+
+@pytest.mark.parametrize("M,N,K,act", [(128, 128, 64, 0), (256, 256, 256, 0), (384, 128, 128, 1),
+                                       (200, 72, 64, 1), (1024, 256, 256, 1)])
+def test_tc_gemm_matches_torch_fp32(M, N, K, act):
+    torch = pytest.importorskip("torch")
+    import pticm
+    rng = np.random.default_rng(M + N + K)
+    a_bits, a = _bf16_bits(rng.standard_normal((M, K)))
+    b_bits, b = _bf16_bits(rng.standard_normal((N, K)) / np.sqrt(K))
+    bias = rng.standard_normal(N).astype(np.float32)
+    out = np.zeros((M, N), np.float32)
+    L = pticm.lib()
+    L.pticm_tc_gemm_check.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                      C.c_void_p]
+    rc = L.pticm_tc_gemm_check(M, N, K, a_bits.ctypes.data, b_bits.ctypes.data, bias.ctypes.data, act,
+                               out.ctypes.data)
+    assert rc == 0, L.pticm_last_error()
+    ref = (a @ b.T + torch.from_numpy(bias)).numpy()
+    if act == 1:
+        pre = out.copy()
+        assert np.allclose(pre, pre)   # finite
+        ref = ref  # act applies only to the bf16 output; the fp32 output is pre-activation
+    assert np.allclose(out, ref, rtol=1e-4, atol=1e-3), np.abs(out - ref).max()

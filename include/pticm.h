@@ -287,6 +287,55 @@ PTICM_API int pticm_run_noalloc(const pticm_problem* p, const pticm_opts* o, con
 PTICM_API int pticm_tc_gemm_check(int M, int N, int K, const uint16_t* A, const uint16_t* B, const float* bias,
                                   int act, float* C);
 
+/* ------------------------------------------------------------ batching -- */
+/* Many instances (problems of any sizes, same nt and chains) in one
+ * persistent cooperative launch: instance i is split over g_i co-resident
+ * blocks that meet at its own group barrier, and every block runs its
+ * (instance, rank) jobs in one global order.  Each instance draws its own
+ * random streams (its index in the batch is part of every RNG counter).
+ * The reference runs one problem per process (src/main.cc:15-209); its
+ * unused folder loop (src/main.cc:149-207) is the batch front end this
+ * replaces.  replicas_per_block in the options caps the replicas of a block
+ * (0: the autotuner decides). */
+typedef struct pticm_batch pticm_batch;
+typedef struct pticm_batch_info {
+    uint32_t count, lanes, chunk, jobs, smem_bytes, threads, tuned;
+    double makespan_us;     /* predicted device time of one PT step of all instances */
+    uint64_t pt_steps, attempts;
+    double last_run_ms;
+} pticm_batch_info;
+PTICM_API int pticm_batch_create(const pticm_problem* const* problems, uint32_t count, const pticm_opts* o,
+                                 pticm_batch** out);
+PTICM_API void pticm_batch_destroy(pticm_batch* b);
+/* count * nt inverse temperatures, row i for instance i; nc as pticm_set_ladder. */
+PTICM_API int pticm_batch_set_ladders(pticm_batch* b, const double* beta, uint32_t nt, int32_t nc);
+PTICM_API int pticm_batch_init_states(pticm_batch* b, uint64_t seed);
+/* Runs trial_steps PT steps at up to three group sizes per instance, restores
+ * the states, and keeps the groups with the shortest predicted makespan. */
+PTICM_API int pticm_batch_autotune(pticm_batch* b, uint32_t trial_steps);
+PTICM_API int pticm_batch_run(pticm_batch* b, uint64_t pt_steps, uint32_t phase_mask);
+PTICM_API int pticm_batch_get_info(pticm_batch* b, pticm_batch_info* info);
+/* per instance: blocks, step time (us; measured once tuned), adjacency staged, ICM teams */
+PTICM_API int pticm_batch_get_groups(pticm_batch* b, uint32_t* group, double* step_us, int32_t* staged,
+                                     int32_t* teams);
+/* per instance: best energy (DBL_MAX before any accepted flip) and accepted flips */
+PTICM_API int pticm_batch_get_best(pticm_batch* b, double* energy, uint64_t* flips);
+PTICM_API int pticm_batch_get_best_state(pticm_batch* b, uint32_t inst, uint8_t* state);
+PTICM_API int pticm_batch_get_swap_stats(pticm_batch* b, uint32_t inst, uint64_t* attempts, uint64_t* successes);
+PTICM_API int pticm_batch_get_energies(pticm_batch* b, uint32_t inst, int64_t* energy, uint32_t* slot_to_replica);
+PTICM_API int pticm_batch_verify(pticm_batch* b, uint64_t* mismatches);
+/* Per-slot energy histograms for every instance (as pticm_enable_energy_histograms). */
+PTICM_API int pticm_batch_enable_energy_histograms(pticm_batch* b, uint64_t from_step);
+/* R rows of nbins counts of one instance (bin b: energy e_lo + 2b); hist may
+ * be NULL to query the sizes. */
+PTICM_API int pticm_batch_get_energy_histograms(pticm_batch* b, uint32_t inst, uint32_t* hist, int64_t* e_lo,
+                                                uint64_t* nbins);
+/* The FP64 multihistogram ln g of one instance from its histograms
+ * (temperatures merged over chains; make_histogram and get_partition_iterate,
+ * src/cae_estimator.cc:45-69,228-253).  Bin k is energy min_emin + k*estep. */
+PTICM_API int pticm_batch_logdos(pticm_batch* b, uint32_t inst, double estep, double* logdos, uint64_t cap,
+                                 uint64_t* nbins, double* min_emin, uint64_t* iterations);
+
 /* ------------------------------------------- surrogate ln g(E) network -- */
 /* A multilayer perceptron f(features, e) -> ln g / N: 7 inputs, four hidden
  * layers of 256 SiLU units, one linear output; BF16 weights and activations

@@ -123,12 +123,14 @@ extern "C" int pticm_run_noalloc(const pticm_problem* p, const pticm_opts* o, co
     LaunchConfig cfg;
     std::string msg;
     if (int rc = choose_config(P, *o, false, D, cfg, msg)) return noalloc_fail(rc, msg);
+    finish_desc(D, P, *o, cfg);
 
     // carve the scratch array
     const size_t n = (size_t)D.n, npad = (size_t)D.n_pad, nnz = (size_t)D.nnz, RR = (size_t)R;
     Carve cv;
     const size_t o_status = cv.take(sizeof(DevStatus)), o_abort = cv.take(sizeof(int)), o_bar = cv.take(2 * sizeof(unsigned));
-    const size_t o_desc = cv.take(sizeof(InstanceDesc)), o_binst = cv.take((size_t)cfg.group * 4), o_rinst = cv.take(RR * 4);
+    const size_t o_desc = cv.take(sizeof(InstanceDesc)), o_soff = cv.take(((size_t)cfg.group + 1) * 4),
+                 o_sched = cv.take((size_t)cfg.group * 8), o_rinst = cv.take(RR * 4);
     const size_t o_row = cv.take((n + 5) * 4), o_adj = cv.take((nnz + 4) * 4), o_col = cv.take(((size_t)D.ncolors + 5) * 4);
     const size_t o_h = cv.take((n + 4) * 4), o_perm = cv.take((n + 4) * 4), o_beta = cv.take((size_t)nt * 8);
     const size_t o_thr = cv.take(thr.size() * 4 + 16);
@@ -147,12 +149,14 @@ extern "C" int pticm_run_noalloc(const pticm_problem* p, const pticm_opts* o, co
     cudaStream_t st = static_cast<cudaStream_t>(stream);
 
     // inputs of the engine layout: host-built tables copied into the array
-    std::vector<int32_t> binst(cfg.group, 0), rinst(RR, 0), perm(P.perm);
+    std::vector<int32_t> soff, sched, rinst(RR, 0), perm(P.perm);
+    single_instance_schedule(cfg.group, soff, sched);
     std::vector<uint32_t> slot0(RR), order0(nt, 0);
     for (int r = 0; r < R; r++) slot0[r] = (uint32_t)r;
     for (uint32_t k = 0; k + 1 < nt; k++) order0[k] = k;
     NA_CK(cudaMemcpyAsync(base + o_desc, &D, sizeof(D), cudaMemcpyHostToDevice, st));
-    NA_CK(cudaMemcpyAsync(base + o_binst, binst.data(), binst.size() * 4, cudaMemcpyHostToDevice, st));
+    NA_CK(cudaMemcpyAsync(base + o_soff, soff.data(), soff.size() * 4, cudaMemcpyHostToDevice, st));
+    NA_CK(cudaMemcpyAsync(base + o_sched, sched.data(), sched.size() * 4, cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemcpyAsync(base + o_rinst, rinst.data(), rinst.size() * 4, cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemcpyAsync(base + o_row, P.drow.data(), P.drow.size() * 4, cudaMemcpyHostToDevice, st));
     if (nnz) NA_CK(cudaMemcpyAsync(base + o_adj, P.dadj.data(), nnz * 4, cudaMemcpyHostToDevice, st));
@@ -181,7 +185,8 @@ extern "C" int pticm_run_noalloc(const pticm_problem* p, const pticm_opts* o, co
 
     EngineArgs A{};
     A.desc = reinterpret_cast<const InstanceDesc*>(base + o_desc);
-    A.block_inst = reinterpret_cast<const int32_t*>(base + o_binst);
+    A.sched_off = reinterpret_cast<const int32_t*>(base + o_soff);
+    A.sched = reinterpret_cast<const int32_t*>(base + o_sched);
     A.n_inst = 1;
     A.n_blocks = cfg.group;
     A.row = reinterpret_cast<const int32_t*>(base + o_row);

@@ -257,7 +257,7 @@ __device__ void icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOC
         }
     }
     if (threadIdx.x == 0) P.subtick(PROF_ICM_SEED);
-    const int algo = A.flags & ENGINE_ICM_MASK;
+    const int algo = D.icm_algo;
     if (cnt > 0 && algo != ENGINE_ICM_BFS) {
         // label the components of the whole overlap subgraph, then flip the
         // sites sharing the seed's label
@@ -435,7 +435,9 @@ __device__ void colored_sweep(const EngineArgs& A, const BlockCtx& B, unsigned l
     const uint32_t* adj = B.adj;
     const int kmax = D.kmax;
     ThreadRng12 rng;
-    rng.start(stream_key(A.seed, STREAM_SWEEP), blockIdx.x * blockDim.x + tid, sweep_idx);
+    // counter: (rank in the group, thread), sweep, instance id in the high
+    // half of the call word (a thread makes far fewer than 2^16 calls)
+    rng.start(stream_key(A.seed, STREAM_SWEEP), (uint32_t)(B.rank * T + tid), sweep_idx, (uint32_t)D.inst_id << 16);
     int acc_de = 0;
     unsigned acc_fl = 0;
     for (int c = 0; c < D.ncolors; c++) {
@@ -804,16 +806,23 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
     extern __shared__ __align__(128) uint8_t smem[];
     const SmemPlan& S = A.sm;
     const int tid = threadIdx.x, T = blockDim.x;
+    volatile int* abortf = A.abort_flag;
+    uint64_t* mbar = sm_ptr<uint64_t>(smem, S.mbar);
+    if (S.stage_adj) {
+        if (tid == 0) mbar_init(mbar, 1);
+        __syncthreads();
+    }
+    uint32_t bulk_parity = 0;
+    const int job_end = A.sched_off[blockIdx.x + 1];
+    for (int job = A.sched_off[blockIdx.x]; job < job_end; job++) {
     BlockCtx B;
-    const int inst = A.block_inst[blockIdx.x];
+    const int inst = A.sched[2 * job];
     B.D = A.desc[inst];
     const InstanceDesc& D = B.D;
-    B.rank = blockIdx.x - D.first_block;
+    B.rank = A.sched[2 * job + 1];
     B.r0 = B.rank * D.rpc;
     const int n = D.n, npad = D.n_pad, R = D.R, nt = D.nt, rpc = D.rpc, kst = D.kmax + 1;
-    volatile int* abortf = A.abort_flag;
 
-    uint64_t* mbar = sm_ptr<uint64_t>(smem, S.mbar);
     int32_t* s_col = sm_ptr<int32_t>(smem, S.col);
     int32_t* s_h = sm_ptr<int32_t>(smem, S.h);
     B.spin = sm_ptr<int8_t>(smem, S.spin);
@@ -848,12 +857,20 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
     B.h = D.has_h ? s_h : nullptr;
 
     // ---- stage the adjacency (bulk copies) and load the block's state
-    if (S.stage_adj) {
+    bool staged = S.stage_adj && D.stage;
+    if (staged && ((reinterpret_cast<uintptr_t>(g_row) | reinterpret_cast<uintptr_t>(g_adj)) & 15u)) {
+        // a bulk copy needs 16-byte aligned sources: record and skip it
+        if (tid == 0) dev_fail(A.status, A.abort_flag, DEV_BAD_INDEX, 3, blockIdx.x, inst);
+        staged = false;
+    }
+    if (staged) {
         int32_t* s_row = sm_ptr<int32_t>(smem, S.row);
         uint32_t* s_adj = sm_ptr<uint32_t>(smem, S.adj);
-        if (tid == 0) mbar_init(mbar, 1);
-        __syncthreads();
         if (tid == 0) {
+            // the previous job's generic-proxy reads of this region are done
+            // (block barrier at the end of every job); order them before the
+            // bulk copy's writes
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             const uint32_t rb = (uint32_t)(((n + 1) * 4 + 15) & ~15);
             const uint32_t ab = (uint32_t)((D.nnz * 4 + 15) & ~15);
             mbar_expect_tx(mbar, rb + ab);
@@ -907,8 +924,10 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
             B.tb[r - B.r0] = (int)(((uint32_t)s % (uint32_t)nt) * (uint32_t)kst);
         }
     }
-    if (S.stage_adj) {
-        if (!mbar_wait_bounded(mbar, 0) && tid == 0) dev_fail(A.status, A.abort_flag, DEV_TMA_TIMEOUT, 2, blockIdx.x, 0);
+    if (staged) {
+        if (!mbar_wait_bounded(mbar, bulk_parity) && tid == 0)
+            dev_fail(A.status, A.abort_flag, DEV_TMA_TIMEOUT, 2, blockIdx.x, inst);
+        bulk_parity ^= 1u;
     }
     __syncthreads();
 
@@ -917,7 +936,9 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
     P.init((A.prof != nullptr) && tid == 0);
     const long long t_start = P.mark;
     const bool best_pp = (A.flags & ENGINE_BEST_PER_PHASE) != 0;
+    unsigned long long t_step1 = 0;
     for (int ls = 0; ls < A.nsteps; ls++) {
+        if (ls == 1 && tid == 0) t_step1 = globaltimer_ns();
         if (tid == 0) s_misc[3] = *abortf;
         __syncthreads();
         if (s_misc[3]) break;
@@ -949,10 +970,11 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
             __syncthreads();
         }
         P.tick(PROF_BARRIER);
-        if (A.hist != nullptr && step >= A.hist_from && B.rank == 0) {
+        if (A.hist != nullptr && D.hist_nbins > 0 && step >= A.hist_from && B.rank == 0) {
             for (int k = tid; k < R; k += T) {
-                const long long bin = (B.E[B.slot[k]] - A.hist_lo) >> 1;
-                if (bin >= 0 && bin < A.hist_nbins) atomicAdd(A.hist + (long long)k * A.hist_nbins + bin, 1u);
+                const long long bin = (B.E[B.slot[k]] - D.hist_lo) >> 1;
+                if (bin >= 0 && bin < D.hist_nbins)
+                    atomicAdd(A.hist + D.hist_off + (long long)k * D.hist_nbins + bin, 1u);
             }
             __syncthreads();
         }
@@ -975,7 +997,7 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
             const int npairs = D.nc * (D.chains / 2);
             if (BLOCKTEAM) {
                 Team<true> team{tid, T, s_team_acc, s_team_bc};
-                const IcmScratch X = icm_scratch(s_icm, S.max_n_pad);
+                const IcmScratch X = icm_scratch(s_icm, npad);
                 for (int q = 0; q < npairs; q++) {
                     const int cp = q / D.nc, kk = q - cp * D.nc, k = nt - 1 - kk;
                     const int rA = (int)B.slot[(2 * cp) * nt + k], rB = (int)B.slot[(2 * cp + 1) * nt + k];
@@ -985,10 +1007,10 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
                 }
             } else {
                 const int warp = tid >> 5, lane = tid & 31;
-                const int teams = min(S.teams, T >> 5);
+                const int teams = min(D.teams, T >> 5);
                 if (warp < teams) {
                     Team<false> team{lane, 32, s_team_acc + warp, s_team_bc + 2 * warp};
-                    const IcmScratch X = icm_scratch(s_icm + (size_t)warp * S.icm_team_bytes, S.max_n_pad);
+                    const IcmScratch X = icm_scratch(s_icm + (size_t)warp * icm_team_bytes(npad), npad);
                     int e = 0;
                     for (int q = 0; q < npairs; q++) {
                         const int cp = q / D.nc, kk = q - cp * D.nc, k = nt - 1 - kk;
@@ -1005,6 +1027,7 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
         P.tick(PROF_ICM);
     }
     __syncthreads();
+    if (A.job_ns != nullptr && tid == 0 && A.nsteps > 1) A.job_ns[job] = globaltimer_ns() - t_step1;
     if (P.on) {
         P.c[PROF_TOTAL] = clock64() - t_start;
         for (int q = 0; q < PROF_PHASES; q++) A.prof[(size_t)blockIdx.x * PROF_PHASES + q] += (unsigned long long)P.c[q];
@@ -1030,6 +1053,9 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
             A.successes[D.rep_off + r] += s_succ[r];
         }
         for (int k = tid; k < nt; k += T) A.xorder[D.rep_off + k] = s_order[k];
+    }
+    // the next job restages shared memory
+    __syncthreads();
     }
 }
 

@@ -124,13 +124,13 @@ struct ThreadRng12 {
     uint4 b0, b1, b2;
     uint32_t avail;
     uint32_t calls;
-    uint4 ctr;   // (thread id, sweep lo, sweep hi, block index)
+    uint4 ctr;   // (thread id, sweep lo, sweep hi, call index)
     uint2 key;
 
-    __device__ __forceinline__ void start(uint2 k, uint32_t tid, unsigned long long sweep) {
+    __device__ __forceinline__ void start(uint2 k, uint32_t tid, unsigned long long sweep, uint32_t call0 = 0u) {
         key = k;
         ctr = make_uint4(tid, (uint32_t)sweep, (uint32_t)(sweep >> 32), 0u);
-        calls = 0;
+        calls = call0;
         refill();
     }
     __device__ __forceinline__ void refill() {

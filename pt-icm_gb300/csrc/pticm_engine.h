@@ -30,8 +30,11 @@ struct InstanceDesc {
     int32_t group;      // blocks that share this instance
     int32_t rpc;        // replicas per block (R = group * rpc)
     int32_t first_block;
-    int32_t inst_id;    // stable id used in RNG counters
-    int32_t pad0, pad1;
+    int32_t inst_id;    // stable id used in RNG counters (< 65536)
+    int32_t icm_algo;   // ENGINE_ICM_* cluster search of this instance
+    int32_t stage;      // 1: adjacency staged into shared memory by bulk copy
+    int32_t teams;      // ICM warp teams of a block (scratch of icm_team_bytes(n_pad) each)
+    int32_t pad0;
     int64_t row_off;    // int32 pool: n+1 row starts (relative to the instance)
     int64_t adj_off;    // uint32 pool: nnz packed entries (col << 8 | (uint8)J)
     int64_t col_off;    // int32 pool: ncolors+1 colour-class starts
@@ -42,6 +45,11 @@ struct InstanceDesc {
     int64_t rep_off;    // first replica of the instance in the replica pools
     int64_t spin_off;   // first byte of the instance in the spin pools
     int64_t perm_off;   // int32 pool: original site -> device site (replay)
+    // optional energy histogram rows (R rows of hist_nbins bins at hist_off of
+    // the launch's histogram pool; bin b holds E = hist_lo + 2b); 0 bins: none
+    int64_t hist_off;
+    int64_t hist_lo;
+    int64_t hist_nbins;
 };
 
 // Shared-memory plan of a launch (bytes), identical for every block.
@@ -77,7 +85,12 @@ struct ReplayArgs {
 
 struct EngineArgs {
     const InstanceDesc* desc;
-    const int32_t* block_inst;    // block -> instance
+    // schedule: block b runs jobs sched_off[b] .. sched_off[b+1]-1 in order;
+    // job j is instance sched[2j] as rank sched[2j+1] of its group.  Every
+    // block lists its jobs in one global order, so the blocks of a group
+    // meet at the group barrier (all blocks are co-resident).
+    const int32_t* sched_off;
+    const int32_t* sched;
     int32_t n_inst;
     int32_t n_blocks;
     // graph pools
@@ -118,12 +131,12 @@ struct EngineArgs {
     int32_t flags;                // ENGINE_* flags
     unsigned long long seed;
     unsigned long long* prof;     // optional: per block, clock64 cycles per phase (PROF_PHASES)
+    unsigned long long* job_ns;   // optional: per job, ns from the start of its step 1 to its end
     // optional per-slot energy histograms (the pilot run of the multihistogram
-    // ladder): after the sweeps of every step >= hist_from, slot k counts the
-    // energy E of its replica in bin (E - hist_lo) / 2 of row k
+    // ladder): after the sweeps of every step >= hist_from, slot k of an
+    // instance counts the energy E of its replica in bin (E - hist_lo) / 2 of
+    // its row k (InstanceDesc::hist_*)
     unsigned int* hist;
-    long long hist_lo;
-    long long hist_nbins;
     unsigned long long hist_from;
     SmemPlan sm;
     ReplayArgs replay;
@@ -139,6 +152,12 @@ enum EngineFlags : int32_t {
     ENGINE_ICM_LABEL_PROP = 16,
     ENGINE_ICM_MASK = 24,
 };
+
+// Shared-memory scratch of one ICM team for an instance of n_pad sites: BFS
+// queue / labels (4 B per site), overlap flags (1 B per site), visited bits.
+inline constexpr uint32_t icm_team_bytes(int32_t n_pad) {
+    return (uint32_t)((((uint64_t)n_pad * 5 + 4 * (((uint64_t)n_pad + 31) / 32)) + 15) & ~15ull);
+}
 
 enum PhaseBits : int32_t { PHASE_SWEEP = 1, PHASE_EXCHANGE = 2, PHASE_ICM = 4 };
 

@@ -55,46 +55,6 @@ int fail(int code, const std::string& m) {
         if (e_ != cudaSuccess) return fail(PTICM_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-constexpr long long kNoBest = std::numeric_limits<long long>::max();
-constexpr uint32_t kSmemLimit = 232448 - 1024;   // 227 KB opt-in per block, less static smem
-
-template <typename T>
-struct DArr {
-    T* p = nullptr;
-    size_t n = 0;
-    DArr() = default;
-    DArr(const DArr&) = delete;
-    DArr& operator=(const DArr&) = delete;
-    ~DArr() { release(); }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-    cudaError_t alloc(size_t count) {
-        release();
-        n = count;
-        if (count == 0) return cudaSuccess;
-        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
-        if (e != cudaSuccess) { p = nullptr; n = 0; return e; }
-        return cudaMemset(p, 0, count * sizeof(T));
-    }
-    cudaError_t upload(const std::vector<T>& v, size_t extra = 0) {
-        cudaError_t e = alloc(v.size() + extra);
-        if (e != cudaSuccess || v.empty()) return e;
-        return cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
-    }
-    cudaError_t download(std::vector<T>& v) const {
-        v.resize(n);
-        if (!n) return cudaSuccess;
-        return cudaMemcpy(v.data(), p, n * sizeof(T), cudaMemcpyDeviceToHost);
-    }
-};
-
-uint32_t align16(uint64_t x) { return (uint32_t)((x + 15) & ~15ull); }
-
-int32_t pad16(int64_t n) { return (int32_t)((n + 15) & ~15ll); }
-
 int check_device() {
     int count = 0;
     cudaError_t e = cudaGetDeviceCount(&count);
@@ -129,7 +89,7 @@ struct pticm_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // device pools
     DArr<InstanceDesc> d_desc;
-    DArr<int32_t> d_block_inst, d_rep_inst, d_row, d_col, d_h, d_perm;
+    DArr<int32_t> d_sched_off, d_sched, d_rep_inst, d_row, d_col, d_h, d_perm;
     DArr<uint32_t> d_adj, d_thr, d_slot, d_order, d_cursor;
     DArr<double> d_beta, d_ptab;
     DArr<int8_t> d_spins, d_pub, d_best_state;
@@ -153,8 +113,30 @@ struct pticm_ctx {
 
 namespace pticm {
 
-// Shared-memory layout for a launch; every region starts on 16 bytes.
-SmemPlan make_plan(const InstanceDesc& D, bool replay, int teams, int threads, bool stage_adj) {
+void PlanDims::add(const InstanceDesc& D, bool stage_this, int teams_of_instance) {
+    const uint64_t kst = (uint64_t)D.kmax + 1, m = (uint64_t)std::max(D.nt - 1, 1);
+    if (stage_this) {
+        stage = true;
+        n_stage = std::max(n_stage, (uint64_t)D.n);
+        nnz_stage = std::max(nnz_stage, (uint64_t)D.nnz);
+    }
+    ncolors = std::max(ncolors, (uint64_t)D.ncolors);
+    if (D.has_h) n_h = std::max(n_h, (uint64_t)D.n);
+    spin_sites = std::max(spin_sites, (uint64_t)D.rpc * (uint64_t)D.n_pad);
+    nt_kst = std::max(nt_kst, (uint64_t)D.nt * kst);
+    R = std::max(R, (uint64_t)D.R);
+    rpc = std::max(rpc, (uint64_t)D.rpc);
+    nt = std::max(nt, (uint64_t)D.nt);
+    chains_m = std::max(chains_m, (uint64_t)D.chains * m);
+    icm_bytes = std::max(icm_bytes, (uint64_t)teams_of_instance * icm_team_bytes(D.n_pad));
+    teams = std::max(teams, teams_of_instance);
+    max_n_pad = std::max(max_n_pad, (uint64_t)D.n_pad);
+    max_kmax = std::max(max_kmax, (uint64_t)D.kmax);
+}
+
+// Shared-memory layout for a launch; every region starts on 16 bytes and is
+// the largest any instance of the launch needs.
+SmemPlan layout_plan(const PlanDims& d) {
     SmemPlan S{};
     uint64_t off = 0;
     auto take = [&](uint64_t bytes) {
@@ -162,48 +144,53 @@ SmemPlan make_plan(const InstanceDesc& D, bool replay, int teams, int threads, b
         off = align16(off + bytes);
         return o;
     };
-    const int kst = D.kmax + 1, m = std::max(D.nt - 1, 1);
     S.mbar = take(16);
-    S.stage_adj = stage_adj ? 1 : 0;
-    if (stage_adj) {
-        S.row = take(align16((uint64_t)(D.n + 1) * 4));
-        S.adj = take(align16((uint64_t)D.nnz * 4));
+    S.stage_adj = d.stage ? 1 : 0;
+    if (d.stage) {
+        S.row = take(align16((d.n_stage + 1) * 4));
+        S.adj = take(align16(d.nnz_stage * 4));
     }
-    S.col = take((uint64_t)(D.ncolors + 1) * 4);
-    S.h = take((uint64_t)D.n * 4);
-    S.spin = take((uint64_t)D.rpc * D.n_pad);
-    S.field = take((uint64_t)D.rpc * D.n_pad * 4);
-    S.thr = take((uint64_t)D.nt * kst * 4);
-    S.ptab = take(replay ? (uint64_t)D.nt * kst * 8 : 0);
-    S.slot = take((uint64_t)D.R * 4);
-    S.rslot = take((uint64_t)D.rpc * 8);
-    S.order = take((uint64_t)D.nt * 4);
-    S.beta = take((uint64_t)D.nt * 8);
-    S.dbeta = take((uint64_t)D.nt * 8);
-    S.E = take((uint64_t)D.R * 8);
-    S.dEp = take((uint64_t)D.rpc * 4);
-    S.flp = take((uint64_t)D.rpc * 4);
-    S.bestE = take((uint64_t)D.rpc * 8);
-    S.flips = take((uint64_t)D.rpc * 8);
-    S.improved = take((uint64_t)D.rpc * 4);
-    S.att = take((uint64_t)D.R * 4);
-    S.succ = take((uint64_t)D.R * 4);
-    S.xlogu = take((uint64_t)D.chains * m * 4 + 16);
-    S.xrand = take((uint64_t)D.chains * m * 4 + 16);
-    S.xlevel = take((uint64_t)D.nt * 4);
-    S.xpos = take((uint64_t)D.nt * 4);
-    // BFS queue (4 B/site), overlap flags (1 B/site), visited bits (n_pad is a multiple of 16)
-    S.icm_team_bytes = align16((uint64_t)D.n_pad * 5 + 4 * ((uint64_t)(D.n_pad + 31) / 32));
-    S.teams = teams;
-    S.icm = take((uint64_t)teams * S.icm_team_bytes);
+    S.col = take((d.ncolors + 1) * 4);
+    S.h = take(d.n_h * 4);
+    S.spin = take(d.spin_sites);
+    S.field = take(d.spin_sites * 4);
+    S.thr = take(d.nt_kst * 4);
+    S.ptab = take(d.replay ? d.nt_kst * 8 : 0);
+    S.slot = take(d.R * 4);
+    S.rslot = take(d.rpc * 8);
+    S.order = take(d.nt * 4);
+    S.beta = take(d.nt * 8);
+    S.dbeta = take(d.nt * 8);
+    S.E = take(d.R * 8);
+    S.dEp = take(d.rpc * 4);
+    S.flp = take(d.rpc * 4);
+    S.bestE = take(d.rpc * 8);
+    S.flips = take(d.rpc * 8);
+    S.improved = take(d.rpc * 4);
+    S.att = take(d.R * 4);
+    S.succ = take(d.R * 4);
+    S.xlogu = take(d.chains_m * 4 + 16);
+    S.xrand = take(d.chains_m * 4 + 16);
+    S.xlevel = take(d.nt * 4);
+    S.xpos = take(d.nt * 4);
+    S.icm_team_bytes = icm_team_bytes((int32_t)d.max_n_pad);
+    S.teams = d.teams;
+    S.icm = take(d.icm_bytes);
     S.misc = take(64 + 8 * 32 + 4 * 64 + 64);
     S.total = (uint32_t)off;
-    S.max_n_pad = D.n_pad;
-    S.max_kmax = D.kmax;
-    S.max_R = D.R;
-    S.max_nt = D.nt;
-    (void)threads;
+    S.max_n_pad = (int32_t)d.max_n_pad;
+    S.max_kmax = (int32_t)d.max_kmax;
+    S.max_R = (int32_t)d.R;
+    S.max_nt = (int32_t)d.nt;
     return S;
+}
+
+SmemPlan make_plan(const InstanceDesc& D, bool replay, int teams, int threads, bool stage_adj) {
+    PlanDims d;
+    d.replay = replay;
+    d.add(D, stage_adj, teams);
+    (void)threads;
+    return layout_plan(d);
 }
 
 // Choose replicas per block, block size, ICM teams and the smem plan for an
@@ -258,6 +245,7 @@ int choose_config(const HostProblem& P, const pticm_opts& o, bool replay, Instan
     }
     D.rpc = rpc;
     D.group = group;
+    D.teams = teams;
     cfg.rpc = rpc;
     cfg.group = group;
     cfg.threads = threads;
@@ -287,6 +275,32 @@ int engine_flags(const HostProblem& P, const pticm_opts& o) {
     else if (o.icm_algo == 2) algo = ENGINE_ICM_UNION_FIND;
     else if (o.icm_algo == 3) algo = ENGINE_ICM_LABEL_PROP;
     return (o.best_per_phase ? ENGINE_BEST_PER_PHASE : 0) | (o.exchange == 1 ? ENGINE_EXCHANGE_EVEN_ODD : 0) | algo;
+}
+
+long long energy_bound(const HostProblem& P) {
+    long long directed = 0, lin = 0;
+    for (int64_t i = 0; i < P.n; i++) {
+        lin += std::llabs((long long)P.h[i]);
+        for (int64_t a = P.row[i]; a < P.row[i + 1]; a++) directed += std::llabs((long long)P.w[a]);
+    }
+    return directed / 2 + lin;
+}
+
+void single_instance_schedule(int group, std::vector<int32_t>& sched_off, std::vector<int32_t>& sched) {
+    sched_off.resize((size_t)group + 1);
+    sched.resize(2 * (size_t)group);
+    for (int b = 0; b <= group; b++) sched_off[b] = b;
+    for (int b = 0; b < group; b++) {
+        sched[2 * b] = 0;
+        sched[2 * b + 1] = b;
+    }
+}
+
+void finish_desc(InstanceDesc& D, const HostProblem& P, const pticm_opts& o, const LaunchConfig& cfg) {
+    D.icm_algo = engine_flags(P, o) & ENGINE_ICM_MASK;
+    D.stage = cfg.plan.stage_adj;
+    D.rpc = cfg.rpc;
+    D.group = cfg.group;
 }
 
 // Acceptance tables of a ladder: thr = ceil(exp(-beta*dE) 2^32) (all-ones:
@@ -331,8 +345,11 @@ int configure(pticm_ctx* c, bool replay) {
     c->teams = cfg.teams;
     c->block_team = cfg.block_team;
     c->plan = cfg.plan;
-    std::vector<int32_t> bi(cfg.group, 0);
-    CK(c->d_block_inst.upload(bi));
+    finish_desc(c->desc, c->P, c->o, cfg);
+    std::vector<int32_t> soff, sched;
+    single_instance_schedule(cfg.group, soff, sched);
+    CK(c->d_sched_off.upload(soff));
+    CK(c->d_sched.upload(sched));
     CK(c->d_desc.upload(std::vector<InstanceDesc>{c->desc}));
     return PTICM_OK;
 }
@@ -340,7 +357,8 @@ int configure(pticm_ctx* c, bool replay) {
 EngineArgs make_args(pticm_ctx* c) {
     EngineArgs A{};
     A.desc = c->d_desc.p;
-    A.block_inst = c->d_block_inst.p;
+    A.sched_off = c->d_sched_off.p;
+    A.sched = c->d_sched.p;
     A.n_inst = 1;
     A.n_blocks = c->group;
     A.row = c->d_row.p;
@@ -375,8 +393,6 @@ EngineArgs make_args(pticm_ctx* c) {
     A.sm = c->plan;
     A.prof = (c->profiling && c->d_prof.n >= (size_t)c->group * PROF_PHASES) ? c->d_prof.p : nullptr;
     A.hist = c->d_hist.p;
-    A.hist_lo = c->hist_lo;
-    A.hist_nbins = c->hist_nbins;
     A.hist_from = c->hist_from;
     A.flags = engine_flags(c->P, c->o);
     return A;
@@ -440,7 +456,7 @@ cudaError_t mhist_iterate(const uint32_t* hist, const uint64_t* hoff, const uint
                           cudaStream_t st);
 }  // namespace pticm
 
-namespace {
+namespace pticm {
 
 // The multihistogram fixed point on the GPU (src/cae_estimator.cc:228-253):
 // iterate until sum_j ((lnZ_j - lnZ'_j)/lnZ'_j)^2 <= 1e-7, as the reference.
@@ -482,6 +498,43 @@ int mhist_dos_impl(const uint32_t* hist, const uint64_t* hoff, const uint64_t* h
     CK(d_dos.download(logdos));
     CK(d_logZ.download(logZ));
     return PTICM_OK;
+}
+
+// Per-slot energy histograms of a pilot run -> multihistogram ln g.  Rows of
+// slot k (chain c = k / nt, temperature j = k % nt) are merged over chains,
+// then cut to [emin_j, emax_j] with bin width estep (make_histogram,
+// src/cae_estimator.cc:45-69); n is the sample count of temperature 0,
+// accumulated into an int as the reference does.
+int slot_hist_dos(const unsigned* rows, int nt, int chains, long long nbins, long long lo, const double* hb,
+                  double estep, std::vector<double>& dos, std::vector<double>& logZ, double& min_emin,
+                  uint64_t& iters) {
+    std::vector<uint64_t> hoff(nt), hlen(nt);
+    std::vector<double> emin(nt), emax(nt);
+    std::vector<uint32_t> hist;
+    std::vector<unsigned> merged((size_t)nbins);
+    for (int j = 0; j < nt; j++) {
+        std::fill(merged.begin(), merged.end(), 0u);
+        for (int c = 0; c < chains; c++) {
+            const unsigned* row = rows + (size_t)(c * nt + j) * (size_t)nbins;
+            for (long long bb = 0; bb < nbins; bb++) merged[bb] += row[bb];
+        }
+        long long first = -1, last = -1;
+        for (long long bb = 0; bb < nbins; bb++)
+            if (merged[bb]) { if (first < 0) first = bb; last = bb; }
+        if (first < 0) return fail(PTICM_ERR_DEVICE, "pilot run recorded no energies");
+        emin[j] = (double)(lo + 2 * first);
+        emax[j] = (double)(lo + 2 * last);
+        hlen[j] = (uint64_t)std::ceil((emax[j] - emin[j]) / estep) + 1;
+        hoff[j] = hist.size();
+        hist.resize(hist.size() + hlen[j], 0);
+        for (long long bb = first; bb <= last; bb++)
+            if (merged[bb]) hist[hoff[j] + (uint64_t)std::floor(((double)(lo + 2 * bb) - emin[j]) / estep)] += merged[bb];
+    }
+    int32_t nacc = 0;   // the reference accumulates row 0 into an int
+    for (uint64_t k = 0; k < hlen[0]; k++) nacc = (int32_t)(nacc + (int32_t)hist[hoff[0] + k]);
+    const double max_emax = *std::max_element(emax.begin(), emax.end());
+    return mhist_dos_impl(hist.data(), hoff.data(), hlen.data(), (uint32_t)nt, hb, emin.data(), estep,
+                          (uint64_t)(int64_t)nacc, max_emax, dos, logZ, min_emin, iters);
 }
 
 }  // namespace
@@ -933,18 +986,15 @@ int pticm_enable_energy_histograms(pticm_ctx* c, uint64_t from_step) {
     if (!c) return fail(PTICM_ERR_INVALID, "null argument");
     // every energy lies in [-W, W], W = sum |J| over edges + sum |h|, and has
     // the parity of W: bins of width 2 from -W are exact energy levels
-    const HostProblem& P = c->P;
-    long long directed = 0, lin = 0;
-    for (int64_t i = 0; i < P.n; i++) {
-        lin += std::llabs((long long)P.h[i]);
-        for (int64_t a = P.row[i]; a < P.row[i + 1]; a++) directed += std::llabs((long long)P.w[a]);
-    }
-    const long long wabs = directed / 2 + lin;
+    const long long wabs = energy_bound(c->P);
     if ((unsigned long long)(wabs + 1) * (unsigned long long)c->R > (1ull << 31))
         return fail(PTICM_ERR_UNSUPPORTED, "energy range too large for per-slot histograms");
     c->hist_lo = -wabs;
     c->hist_nbins = wabs + 1;
     c->hist_from = from_step;
+    c->desc.hist_off = 0;
+    c->desc.hist_lo = c->hist_lo;
+    c->desc.hist_nbins = c->hist_nbins;
     CK(c->d_hist.alloc((size_t)c->R * (size_t)c->hist_nbins));
     return PTICM_OK;
 }
@@ -1017,33 +1067,11 @@ int pticm_cae_ladder(const pticm_problem* p, uint64_t seed, double T0, double T1
     if (int rc = pticm_run(c, burn_in + samples, 7)) return rc;
     std::vector<unsigned> habs;
     CK(c->d_hist.download(habs));
-    // per-temperature histograms over [emin_j, emax_j] with bin width estep
-    // (make_histogram, :45-69)
-    std::vector<uint64_t> hoff(nt), hlen(nt);
-    std::vector<double> emin(nt), emax(nt);
-    std::vector<uint32_t> hist;
-    for (uint32_t j = 0; j < nt; j++) {
-        const unsigned* row = habs.data() + (size_t)j * c->hist_nbins;
-        long long first = -1, last = -1;
-        for (long long bb = 0; bb < c->hist_nbins; bb++)
-            if (row[bb]) { if (first < 0) first = bb; last = bb; }
-        if (first < 0) return fail(PTICM_ERR_DEVICE, "pilot run recorded no energies");
-        emin[j] = (double)(c->hist_lo + 2 * first);
-        emax[j] = (double)(c->hist_lo + 2 * last);
-        hlen[j] = (uint64_t)std::ceil((emax[j] - emin[j]) / estep) + 1;
-        hoff[j] = hist.size();
-        hist.resize(hist.size() + hlen[j], 0);
-        for (long long bb = first; bb <= last; bb++)
-            if (row[bb]) hist[hoff[j] + (uint64_t)std::floor(((double)(c->hist_lo + 2 * bb) - emin[j]) / estep)] += row[bb];
-    }
-    int32_t nacc = 0;   // the reference accumulates row 0 into an int
-    for (uint64_t k = 0; k < hlen[0]; k++) nacc = (int32_t)(nacc + (int32_t)hist[hoff[0] + k]);
-    const double max_emax = *std::max_element(emax.begin(), emax.end());
     std::vector<double> dos, z;
     double min_emin = 0;
     uint64_t it = 0;
-    if (int rc = mhist_dos_impl(hist.data(), hoff.data(), hlen.data(), nt, hb.data(), emin.data(), estep,
-                                (uint64_t)(int64_t)nacc, max_emax, dos, z, min_emin, it))
+    if (int rc = slot_hist_dos(habs.data(), (int)nt, 1, c->hist_nbins, c->hist_lo, hb.data(), estep, dos, z,
+                               min_emin, it))
         return rc;
     *count = cae_walk(dos, min_emin, estep, beta_start, beta_end, step_size, r, nt, beta_out);
     return PTICM_OK;

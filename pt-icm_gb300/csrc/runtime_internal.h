@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <limits>
 #include <string>
 #include <vector>
 
@@ -12,18 +13,82 @@
 
 namespace pticm {
 
+constexpr long long kNoBest = std::numeric_limits<long long>::max();
+
+template <typename T>
+struct DArr {
+    T* p = nullptr;
+    size_t n = 0;
+    DArr() = default;
+    DArr(const DArr&) = delete;
+    DArr& operator=(const DArr&) = delete;
+    ~DArr() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t alloc(size_t count) {
+        release();
+        n = count;
+        if (count == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) { p = nullptr; n = 0; return e; }
+        return cudaMemset(p, 0, count * sizeof(T));
+    }
+    cudaError_t upload(const std::vector<T>& v, size_t extra = 0) {
+        cudaError_t e = alloc(v.size() + extra);
+        if (e != cudaSuccess || v.empty()) return e;
+        return cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    }
+    cudaError_t download(std::vector<T>& v) const {
+        v.resize(n);
+        if (!n) return cudaSuccess;
+        return cudaMemcpy(v.data(), p, n * sizeof(T), cudaMemcpyDeviceToHost);
+    }
+};
+
+inline uint32_t align16(uint64_t x) { return (uint32_t)((x + 15) & ~15ull); }
+
+inline int32_t pad16(int64_t n) { return (int32_t)((n + 15) & ~15ll); }
+
 struct LaunchConfig {
     int rpc = 0, group = 0, threads = 0, teams = 1;
     bool block_team = false;
     SmemPlan plan{};
 };
 
+// Shared-memory needs of the instances of one launch (region-wise maxima).
+struct PlanDims {
+    uint64_t n_stage = 0, nnz_stage = 0, ncolors = 0, n_h = 0, spin_sites = 0, nt_kst = 0, R = 0, rpc = 0, nt = 0,
+             chains_m = 0, icm_bytes = 0, max_n_pad = 0, max_kmax = 0;
+    int teams = 0;
+    bool stage = false, replay = false;
+    void add(const InstanceDesc& D, bool stage_this, int teams_of_instance);
+};
+SmemPlan layout_plan(const PlanDims& d);
 SmemPlan make_plan(const InstanceDesc& D, bool replay, int teams, int threads, bool stage_adj);
+constexpr uint32_t kSmemLimit = 232448 - 1024;   // 227 KB opt-in per block, less static smem
+
 int choose_config(const HostProblem& P, const pticm_opts& o, bool replay, InstanceDesc& D, LaunchConfig& cfg,
                   std::string& msg);
 int engine_flags(const HostProblem& P, const pticm_opts& o);
+// Schedule of a launch that holds one instance: block b runs rank b.
+void single_instance_schedule(int group, std::vector<int32_t>& sched_off, std::vector<int32_t>& sched);
+// Per-instance engine choices of a configured instance: cluster search and
+// adjacency staging.
+void finish_desc(InstanceDesc& D, const HostProblem& P, const pticm_opts& o, const LaunchConfig& cfg);
 int ladder_tables(const HostProblem& P, const double* beta, int nt, int nc_req, bool icm, int chains,
                   std::vector<uint32_t>& thr, std::vector<double>& ptab);
+
+int mhist_dos_impl(const uint32_t* hist, const uint64_t* hoff, const uint64_t* hlen, uint32_t nt,
+                   const double* beta, const double* emin, double estep, uint64_t n, double max_emax,
+                   std::vector<double>& logdos, std::vector<double>& logZ, double& min_emin, uint64_t& iters);
+int slot_hist_dos(const unsigned* rows, int nt, int chains, long long nbins, long long lo, const double* hb,
+                  double estep, std::vector<double>& dos, std::vector<double>& logZ, double& min_emin,
+                  uint64_t& iters);
+// energy range of a problem: every energy lies in [-W, W] with the parity of W
+long long energy_bound(const HostProblem& P);
 
 const HostProblem& problem_host(const pticm_problem* p);
 void set_last_error(const std::string& m);
@@ -31,6 +96,8 @@ void set_last_error(const std::string& m);
 cudaError_t launch_engine(const EngineArgs& A, int threads, bool replay, bool block_team, bool cooperative,
                           cudaStream_t stream);
 cudaError_t engine_max_blocks_per_sm(bool replay, bool block_team, int threads, size_t smem, int* out);
+cudaError_t launch_init_spins(const EngineArgs& A, const int32_t* rep_inst, int total_reps,
+                              unsigned long long seed, cudaStream_t stream);
 cudaError_t launch_recompute(const EngineArgs& A, const int32_t* rep_inst, int total_reps, int write_back,
                              unsigned long long* mismatches, long long* E_out, long long* cut2_out,
                              cudaStream_t stream);

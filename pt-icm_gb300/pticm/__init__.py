@@ -40,6 +40,13 @@ class Opts(C.Structure):
                 ("block_threads", C.c_uint32), ("replicas_per_block", C.c_uint32), ("icm_algo", C.c_uint32)]
 
 
+class BatchInfo(C.Structure):
+    _fields_ = [("count", C.c_uint32), ("lanes", C.c_uint32), ("chunk", C.c_uint32), ("jobs", C.c_uint32),
+                ("smem_bytes", C.c_uint32), ("threads", C.c_uint32), ("tuned", C.c_uint32),
+                ("makespan_us", C.c_double), ("pt_steps", C.c_uint64), ("attempts", C.c_uint64),
+                ("last_run_ms", C.c_double)]
+
+
 class Stats(C.Structure):
     _fields_ = [("pt_steps", C.c_uint64), ("attempts", C.c_uint64), ("flips", C.c_uint64),
                 ("swaps", C.c_uint64), ("nt", C.c_uint32), ("chains", C.c_uint32), ("nc", C.c_uint32),
@@ -92,6 +99,29 @@ def lib():
         "pticm_mhist_dos": [P, P, P, u32, P, P, dbl, u64, dbl, P, u64, P, P, P],
         "pticm_cae_walk": [P, u64, dbl, dbl, dbl, dbl, dbl, dbl, u32, P, P],
         "pticm_get_profile": [P, P, P],
+        "pticm_tc_gemm_check": [C.c_int, C.c_int, C.c_int, P, P, P, C.c_int, P],
+        "pticm_batch_create": [P, u32, C.POINTER(Opts), C.POINTER(P)],
+        "pticm_batch_set_ladders": [P, P, u32, i32],
+        "pticm_batch_init_states": [P, u64],
+        "pticm_batch_autotune": [P, u32],
+        "pticm_batch_run": [P, u64, u32],
+        "pticm_batch_get_info": [P, C.POINTER(BatchInfo)],
+        "pticm_batch_get_groups": [P, P, P, P, P],
+        "pticm_batch_get_best": [P, P, P],
+        "pticm_batch_get_best_state": [P, u32, P],
+        "pticm_batch_get_swap_stats": [P, u32, P, P],
+        "pticm_batch_get_energies": [P, u32, P, P],
+        "pticm_batch_verify": [P, P],
+        "pticm_batch_enable_energy_histograms": [P, u64],
+        "pticm_batch_get_energy_histograms": [P, u32, P, P, P],
+        "pticm_batch_logdos": [P, u32, dbl, P, u64, P, P, P],
+        "pticm_mlp_create": [u64, u32, C.POINTER(P)],
+        "pticm_mlp_get_params": [P, P],
+        "pticm_mlp_set_params": [P, P],
+        "pticm_mlp_set_data": [P, P, P, u64],
+        "pticm_mlp_gradients": [P, P, P, u32, P, P],
+        "pticm_mlp_train": [P, P, P, u64, u32, C.c_float, u64, P],
+        "pticm_mlp_predict": [P, P, u64, P],
     }
     for name, args in sigs.items():
         f = getattr(L, name)
@@ -103,6 +133,12 @@ def lib():
     L.pticm_destroy.restype = None
     L.pticm_opts_default.argtypes = [C.POINTER(Opts)]
     L.pticm_opts_default.restype = None
+    L.pticm_batch_destroy.argtypes = [P]
+    L.pticm_batch_destroy.restype = None
+    L.pticm_mlp_destroy.argtypes = [P]
+    L.pticm_mlp_destroy.restype = None
+    L.pticm_mlp_param_count.argtypes = []
+    L.pticm_mlp_param_count.restype = u64
     L.pticm_last_error.restype = C.c_char_p
     L.pticm_version.restype = C.c_char_p
     _lib = L
@@ -350,3 +386,147 @@ def solve(problem: Problem, *, seed, Nt, pts, T0=0.6, T1=2.8, inverse=False, icm
                 best_state_sweep=sweep, best_energy=E, best_maxcut=float(cut[0]), num_of_flips=st.flips,
                 num_of_swaps=st.swaps, best_state=state, beta=beta, attempts=st.attempts,
                 device_ms=st.last_run_ms, context=ctx)
+
+
+class MLP:
+    """The surrogate ln g(E) network on the tensor cores (pticm_mlp_*)."""
+
+    def __init__(self, seed=0, batch=1024):
+        self._h = C.c_void_p()
+        _check(lib().pticm_mlp_create(seed, batch, C.byref(self._h)))
+        self.n_params = int(lib().pticm_mlp_param_count())
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.pticm_mlp_destroy(self._h)
+            self._h = None
+
+    @property
+    def params(self):
+        out = np.zeros(self.n_params, np.float32)
+        _check(lib().pticm_mlp_get_params(self._h, _p(out)))
+        return out
+
+    @params.setter
+    def params(self, value):
+        v = np.ascontiguousarray(value, np.float32)
+        assert v.shape == (self.n_params,)
+        _check(lib().pticm_mlp_set_params(self._h, _p(v)))
+
+    def gradients(self, X, y):
+        X = np.ascontiguousarray(X, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        g = np.zeros(self.n_params, np.float32)
+        loss = C.c_float()
+        _check(lib().pticm_mlp_gradients(self._h, _p(X), _p(y), len(y), _p(g), C.byref(loss)))
+        return loss.value, g
+
+    def train(self, X, y, steps, lr=1e-3, seed=0):
+        X = np.ascontiguousarray(X, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        losses = np.zeros(steps, np.float32)
+        _check(lib().pticm_mlp_train(self._h, _p(X), _p(y), len(y), steps, lr, seed, _p(losses)))
+        return losses
+
+    def predict(self, X):
+        X = np.ascontiguousarray(X, np.float32)
+        out = np.zeros(len(X), np.float32)
+        _check(lib().pticm_mlp_predict(self._h, _p(X), len(X), _p(out)))
+        return out
+
+
+class Batch:
+    """Many instances in one persistent launch (pticm_batch_*)."""
+
+    def __init__(self, problems, *, nt, chains=2, seed=1, icm=True, exchange=1, sweeps=1, replicas_per_block=0,
+                 block_threads=0, icm_algo=0):
+        o = Opts()
+        lib().pticm_opts_default(C.byref(o))
+        o.seed, o.nt, o.chains, o.sweeps, o.icm, o.exchange = seed, nt, chains, sweeps, int(icm), exchange
+        o.replicas_per_block, o.block_threads, o.icm_algo = replicas_per_block, block_threads, icm_algo
+        self.problems = list(problems)
+        self.count, self.nt, self.R = len(self.problems), nt, nt * chains
+        arr = (C.c_void_p * self.count)(*[p._h for p in self.problems])
+        self._h = C.c_void_p()
+        _check(lib().pticm_batch_create(arr, self.count, C.byref(o), C.byref(self._h)))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.pticm_batch_destroy(self._h)
+            self._h = None
+
+    def set_ladders(self, beta, nc=-1):
+        b = np.ascontiguousarray(np.broadcast_to(np.asarray(beta, np.float64), (self.count, self.nt)))
+        _check(lib().pticm_batch_set_ladders(self._h, _p(b), self.nt, nc))
+
+    def init_states(self, seed):
+        _check(lib().pticm_batch_init_states(self._h, seed))
+
+    def autotune(self, trial_steps=20):
+        _check(lib().pticm_batch_autotune(self._h, trial_steps))
+
+    def run(self, steps, phase_mask=7):
+        _check(lib().pticm_batch_run(self._h, steps, phase_mask))
+
+    def info(self):
+        i = BatchInfo()
+        _check(lib().pticm_batch_get_info(self._h, C.byref(i)))
+        return i
+
+    def groups(self):
+        g = np.zeros(self.count, np.uint32)
+        t = np.zeros(self.count)
+        st = np.zeros(self.count, np.int32)
+        tm = np.zeros(self.count, np.int32)
+        _check(lib().pticm_batch_get_groups(self._h, _p(g), _p(t), _p(st), _p(tm)))
+        return g, t, st, tm
+
+    def best(self):
+        e = np.zeros(self.count)
+        f = np.zeros(self.count, np.uint64)
+        _check(lib().pticm_batch_get_best(self._h, _p(e), _p(f)))
+        return e, f
+
+    def best_state(self, inst):
+        s = np.zeros(self.problems[inst].info().n, np.uint8)
+        _check(lib().pticm_batch_get_best_state(self._h, inst, _p(s)))
+        return s
+
+    def swap_stats(self, inst):
+        a = np.zeros(self.R, np.uint64)
+        s = np.zeros(self.R, np.uint64)
+        _check(lib().pticm_batch_get_swap_stats(self._h, inst, _p(a), _p(s)))
+        return a, s
+
+    def energies(self, inst):
+        e = np.zeros(self.R, np.int64)
+        sl = np.zeros(self.R, np.uint32)
+        _check(lib().pticm_batch_get_energies(self._h, inst, _p(e), _p(sl)))
+        return e, sl
+
+    def verify(self):
+        m = C.c_uint64()
+        _check(lib().pticm_batch_verify(self._h, C.byref(m)))
+        return m.value
+
+    def enable_energy_histograms(self, from_step):
+        _check(lib().pticm_batch_enable_energy_histograms(self._h, from_step))
+
+    def energy_histograms(self, inst):
+        lo = C.c_int64()
+        nb = C.c_uint64()
+        _check(lib().pticm_batch_get_energy_histograms(self._h, inst, None, C.byref(lo), C.byref(nb)))
+        h = np.zeros((self.R, nb.value), np.uint32)
+        _check(lib().pticm_batch_get_energy_histograms(self._h, inst, _p(h), C.byref(lo), C.byref(nb)))
+        return h, lo.value + 2 * np.arange(nb.value)
+
+    def logdos(self, inst, estep=2.0):
+        hb = C.c_uint64()
+        _check(lib().pticm_batch_get_energy_histograms(self._h, inst, None, None, C.byref(hb)))
+        cap = int(np.ceil(2 * hb.value / estep)) + 2
+        d = np.zeros(cap)
+        nb = C.c_uint64()
+        me = C.c_double()
+        it = C.c_uint64()
+        _check(lib().pticm_batch_logdos(self._h, inst, estep, _p(d), cap, C.byref(nb), C.byref(me), C.byref(it)))
+        return d[:nb.value], me.value, it.value

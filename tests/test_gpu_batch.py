@@ -1,0 +1,165 @@
+"""Batched launches (pticm_batch_*): many instances in one persistent kernel.
+
+* A one-instance batch is the single-instance context, bit for bit (same
+  block layout, same random streams).
+* A batch of uneven instances stays exact: fields and energies equal a
+  from-scratch recomputation after the run; the best energies equal the
+  energies of the best states; the autotuner's trial runs leave the states
+  as they were.
+* Copies of one graph in one batch are independent runs whose per-
+  temperature mean energies and exchange acceptances match the oracle's
+  (the reference's algorithm) within 3 sigma.
+* Per-instance multihistogram ln g equals the oracle's on the same counts.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+G = os.path.join(os.path.dirname(__file__), "golden", "graphs")
+
+
+def _mixed_problems():
+    import pticm
+    from pticm import instances as I
+    insts = [I.pm_lattice(6, seed=3), I.pm_lattice(10, seed=4), I.pm_lattice(16, seed=5),
+             I.random_graph(150, 300, seed=6, signed=True), I.random_graph(300, 1500, seed=7, signed=True),
+             I.random_graph(700, 5600, seed=8, signed=True), I.pm_lattice(32, seed=9)]
+    return [pticm.Problem.from_instance(x) for x in insts]
+
+
+def test_one_instance_batch_equals_context():
+    import pticm
+    prob = pticm.Problem.load(os.path.join(G, "rnd200_w1"))
+    beta = pticm.beta_linspace(0.5, 15.0, 8)
+    ctx = pticm.Context(prob, nt=8, seed=21, icm=True, exchange=1, replicas_per_block=4, block_threads=256)
+    ctx.set_ladder(beta)
+    ctx.init_states(77)
+    ctx.run(300)
+    bat = pticm.Batch([prob], nt=8, seed=21, icm=True, exchange=1, replicas_per_block=4, block_threads=256)
+    bat.set_ladders(beta)
+    bat.init_states(77)
+    bat.run(300)
+    _, Ec, _, slot_c = ctx.replicas()
+    Eb, sl = bat.energies(0)
+    assert np.array_equal(Ec, Eb)
+    _, att_c, suc_c = ctx.stats()
+    att_b, suc_b = bat.swap_stats(0)
+    assert np.array_equal(att_c, att_b) and np.array_equal(suc_c, suc_b)
+    assert bat.best()[0][0] == ctx.best()[0]
+
+
+def test_uneven_batch_is_exact_and_autotune_restores_states():
+    import pticm
+    probs = _mixed_problems()
+    bat = pticm.Batch(probs, nt=8, seed=5, icm=True, exchange=1)
+    bat.set_ladders(pticm.beta_linspace(0.5, 3.0, 8))
+    bat.init_states(9)
+    before = [bat.energies(i)[0].copy() for i in range(len(probs))]
+    bat.autotune(8)
+    info = bat.info()
+    assert info.tuned == 1 and info.lanes >= 1 and info.jobs >= len(probs)
+    for i in range(len(probs)):
+        assert np.array_equal(bat.energies(i)[0], before[i])
+    g, t, staged, teams = bat.groups()
+    assert (g >= 1).all() and (t > 0).all() and (teams >= 1).all()
+    bat.run(400)
+    assert bat.verify() == 0
+    best, flips = bat.best()
+    for i, p in enumerate(probs):
+        s = bat.best_state(i)
+        E, _ = p.evaluate(s[None, :])
+        assert E[0] == best[i]
+        assert flips[i] > 0
+        att, suc = bat.swap_stats(i)
+        assert att.sum() > 0 and suc.sum() > 0
+
+
+def test_copies_in_one_batch_match_reference_statistics():
+    import pticm
+    path = os.path.join(G, "rnd60_pm")
+    nt, pts, burn, seeds = 8, 3000, 800, 12
+    means, rates = [], []
+    for s in range(seeds):
+        o = O.solve(O.Problem.load(path, 300 + s), seed=300 + s, Nt=nt, pts=pts, icm=True, T0=0.5, T1=3.0, trace=True)
+        se = o["trace"]["step_energy"]
+        means.append(se[burn:].reshape(-1, 2, nt).mean(axis=(0, 1)))
+        att = o["swap_attempts"].astype(float)
+        suc = o["swap_successes"].astype(float)
+        rates.append((suc[:nt - 1] + suc[nt:2 * nt - 1]) / np.maximum(att[:nt - 1] + att[nt:2 * nt - 1], 1))
+    om, orate = np.array(means), np.array(rates)
+    prob = pticm.Problem.load(path)
+    bat = pticm.Batch([prob] * seeds, nt=nt, seed=901, icm=True, exchange=1)
+    bat.set_ladders(pticm.beta_linspace(0.5, 3.0, nt))
+    bat.init_states(902)
+    bat.enable_energy_histograms(burn)
+    bat.run(pts)
+    gm, grate = [], []
+    for i in range(seeds):
+        h, e = bat.energy_histograms(i)
+        m = (h * e[None, :]).sum(axis=1) / h.sum(axis=1)
+        gm.append(m.reshape(2, nt).mean(axis=0))
+        att, suc = bat.swap_stats(i)
+        att, suc = att.astype(float), suc.astype(float)
+        grate.append((suc[:nt - 1] + suc[nt:2 * nt - 1]) / np.maximum(att[:nt - 1] + att[nt:2 * nt - 1], 1))
+    gm, grate = np.array(gm), np.array(grate)
+    assert np.std(gm[:, 0]) > 0   # the copies are independent runs
+
+    def z(a, b):
+        sig = np.sqrt(a.var(axis=0, ddof=1) / len(a) + b.var(axis=0, ddof=1) / len(b)) + 1e-12
+        return np.abs(a.mean(axis=0) - b.mean(axis=0)) / sig
+
+    zz = np.concatenate([z(gm, om), z(grate, orate)])
+    assert (zz > 3.0).sum() <= 1, zz
+    assert zz.max() < 4.5, zz
+
+
+def _compact(rows, e, nt, estep=2.0):
+    """make_histogram (src/cae_estimator.cc:45-69) of per-slot rows, chains merged."""
+    chains = rows.shape[0] // nt
+    hist, off, ln, emin, emax = [], [], [], [], []
+    for j in range(nt):
+        m = rows[j::nt][:chains].sum(axis=0) if chains > 1 else rows[j]
+        nz = np.nonzero(m)[0]
+        lo, hi = e[nz[0]], e[nz[-1]]
+        L = int(np.ceil((hi - lo) / estep)) + 1
+        hj = np.zeros(L, np.uint32)
+        for b in nz:
+            hj[int(np.floor((e[b] - lo) / estep))] += m[b]
+        off.append(sum(len(x) for x in hist))
+        hist.append(hj)
+        ln.append(L)
+        emin.append(float(lo))
+        emax.append(float(hi))
+    n = int(hist[0].sum())
+    return np.concatenate(hist), np.array(off, np.uint64), np.array(ln, np.uint64), np.array(emin), max(emax), n
+
+
+def test_batch_logdos_matches_oracle():
+    import pticm
+    names = ["pmL10.gset", "rnd60_pm", "pmL20_c1.gset"]
+    probs = [pticm.Problem.load(os.path.join(G, g)) for g in names]
+    nt = 8
+    bs, be = 1 / 0.6, 1 / 2.8
+    hb = bs + (be - bs) / (nt - 1) * np.arange(nt)
+    bat = pticm.Batch(probs, nt=nt, chains=1, seed=13, icm=False, exchange=0)
+    bat.set_ladders(hb)
+    bat.init_states(14)
+    bat.enable_energy_histograms(300)
+    bat.run(1300)
+    for i in range(len(probs)):
+        rows, e = bat.energy_histograms(i)
+        hist, off, ln, emin, max_emax, n = _compact(rows, e, nt)
+        dos_o, _, _ = O.partition_iterate(hist, off, ln, hb, emin, 2.0, n, max_emax)
+        dos_g, me, _ = bat.logdos(i)
+        assert me == emin.min()
+        assert len(dos_g) == len(dos_o)
+        filled = dos_o > -1e300
+        assert np.array_equal(filled, dos_g > -1e300)
+        shift = np.median(dos_g[filled] - dos_o[filled])
+        assert np.allclose(dos_g[filled] - shift, dos_o[filled], rtol=0,
+                           atol=2e-3 * max(1.0, np.abs(dos_o[filled]).max()))

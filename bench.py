@@ -309,6 +309,230 @@ def run_gpu(args):
     return 0
 
 
+BATCH_COUNT, BATCH_NT, BATCH_PT_PER_STEP = 1024, 32, 100
+BATCH_WORKLOAD = ("1024 uneven instances in one persistent launch: 512 +-J toroidal lattices L in {10,20,32,50}, "
+                  "512 random +-1 graphs N log-uniform 200..5000, mean degree U[3,20] (seeds 1000+i); "
+                  "Nt=32 x 2 chains (R=64) each, T 0.5..3.0 linear in beta, ICM on, groups autotuned, "
+                  "100 PT steps of every instance per bench step")
+
+
+def run_gpu_batched(args):
+    """The batched workload: spin-flip attempts/s over all instances."""
+    import numpy as np
+    import torch
+    import pticm
+    from pticm import instances as I
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    t_gen = time.perf_counter()
+    insts = I.batch_mix(args.batch_count)
+    probs = [pticm.Problem.from_instance(x) for x in insts]
+    t_gen = time.perf_counter() - t_gen
+    beta = pticm.beta_linspace(0.5, 3.0, BATCH_NT)
+    bat = pticm.Batch(probs, nt=BATCH_NT, seed=1, icm=True, exchange=1)
+    bat.set_ladders(beta)
+    bat.init_states(2)
+    t_tune = time.perf_counter()
+    bat.autotune(20)
+    t_tune = time.perf_counter() - t_tune
+    sites = sum(x.n for x in insts) * 2 * BATCH_NT
+    bytes_per_sweep = sum(2 * x.n + 12 * x.m for x in insts) * 2 * BATCH_NT
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        bat.run(BATCH_PT_PER_STEP)
+    if bat.verify():
+        raise RuntimeError("verify found mismatches after warm-up")
+    dev_ms = []
+    wall0 = time.perf_counter()
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            bat.run(BATCH_PT_PER_STEP)
+            dev_ms.append(bat.info().last_run_ms)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    info = bat.info()
+    total_ms = sum(dev_ms)
+    value = sites * BATCH_PT_PER_STEP * args.steps / (total_ms / 1000.0)
+    mism = bat.verify()
+    g, t_us, staged, teams = bat.groups()
+    # end to end: problems from host edge lists, ladders, states, the run and
+    # the per-instance best energies back, per step
+    e2e_t = []
+    h2d = sum(x.src.nbytes + x.dst.nbytes + x.w.nbytes for x in insts) + beta.nbytes * len(insts)
+    for i in range(args.e2e_steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ps = [pticm.Problem.from_coo(x.n, x.src, x.dst, x.w) for x in insts]
+        b2 = pticm.Batch(ps, nt=BATCH_NT, seed=50 + i, icm=True, exchange=1)
+        b2.set_ladders(beta)
+        b2.init_states(60 + i)
+        b2.run(BATCH_PT_PER_STEP)
+        best, flips = b2.best()
+        del b2, ps
+        torch.cuda.synchronize()
+        e2e_t.append(time.perf_counter() - t0)
+    peak, peak_kind = _peaks()
+    launch_s = total_ms / 1000.0 / args.steps
+    achieved = bytes_per_sweep * BATCH_PT_PER_STEP / launch_s / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "attempts/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int8 spins, int32 fields/energies", "data": "synthetic",
+        "config": {"workload": BATCH_WORKLOAD if args.batch_count == BATCH_COUNT else
+                   BATCH_WORKLOAD.replace("1024 uneven", f"{args.batch_count} uneven"),
+                   "instances": len(insts), "sites_per_sweep": sites,
+                   "l2": "flushed between steps (256 MB write); the working set also exceeds L2",
+                   "lanes": info.lanes, "jobs": info.jobs, "chunk_pt_steps": info.chunk, "smem_bytes": info.smem_bytes,
+                   "predicted_makespan_us_per_pt_step": info.makespan_us,
+                   "groups": {str(k): int(v) for k, v in zip(*np.unique(g, return_counts=True))},
+                   "staged_instances": int(staged.sum()), "autotune_s": t_tune, "generate_s": t_gen,
+                   "wall_s": wall, "verify_mismatches_after": mism},
+        "e2e": {"value": sites * BATCH_PT_PER_STEP / statistics.median(e2e_t), "unit": "attempts/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 16 * len(insts),
+                "what": "all problems from host edge lists (colouring on the host) + ladders + states + "
+                        "100 PT steps + per-instance best energies back"},
+        "gpu_launches": args.steps * ((BATCH_PT_PER_STEP + info.chunk - 1) // info.chunk),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None,
+                     "note": f"algorithmic bytes 2N+12M per replica-sweep summed over instances; peak {peak_kind}"},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+LADDER_WORKLOAD = ("learned ladder: 4x256 SiLU MLP (BF16 weights, FP32 accumulate) on instance features + E/W, "
+                   "trained on FP64 multihistogram ln g of synthetic instances (+-J lattices L 6..50, +-1 random "
+                   "graphs N 100..3000, mean degree 3..20); evaluated on held-out instances: ln g error, ladder "
+                   "acceptance (r=0.4, 32 temperatures), ladder cost and time-to-target vs the multihistogram ladder")
+
+
+def _ttt_runs(prob, ladder, target, copies, chunk, max_steps, seed):
+    """PT with ICM on `copies` independent copies of one instance in one
+    batch: the step at which each copy's best energy first reaches target."""
+    import numpy as np
+    import pticm
+    lad = np.sort(np.asarray(ladder))           # ascending: ICM on the coldest (as --sort-ladder)
+    bat = pticm.Batch([prob] * copies, nt=len(lad), seed=seed, icm=True, exchange=1)
+    bat.set_ladders(lad)
+    bat.init_states(seed + 1)
+    hit = np.full(copies, -1, np.int64)
+    done = 0
+    while done < max_steps and (hit < 0).any():
+        bat.run(chunk)
+        done += chunk
+        best, _ = bat.best()
+        newly = (hit < 0) & (best <= target)
+        hit[newly] = done
+    ctx = pticm.Context(prob, nt=len(lad), seed=seed + 2, icm=True)
+    ctx.set_ladder(lad)
+    ctx.init_states(seed + 3)
+    ctx.run(50)
+    ctx.run(400)
+    ms_per_step = ctx.stats()[0].last_run_ms / 400
+    return hit, ms_per_step
+
+
+def run_gpu_ladder(args):
+    import numpy as np
+    import torch
+    import pticm
+    from pticm import instances as I, surrogate as S
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    log = (lambda *a: print(*a, file=sys.stderr, flush=True))
+    t0 = time.perf_counter()
+    train = I.ladder_mix(args.ladder_train, seed0=100)
+    held = I.ladder_mix(args.ladder_held, seed0=900000)
+    t_gen = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    recs = S.make_records(train, nt=32, burn_in=1000, samples=2000, seed=3, log=log)
+    t_data = time.perf_counter() - t0
+    hrec = S.make_records(held, nt=32, burn_in=1000, samples=2000, seed=4, log=log)
+    t0 = time.perf_counter()
+    m, losses = S.train(recs, steps=4000, batch=1024, lr=1e-3, seed=1, log=log)
+    t_train = time.perf_counter() - t0
+    n_rows = len(S.training_arrays(recs)[1])
+    dev = lambda a: float(np.mean(np.abs(a - 0.4)))
+    rows = []
+    for i, (x, r) in enumerate(zip(held, hrec)):
+        p = pticm.Problem.from_instance(x)
+        T0, T1 = S.pilot_range(x)
+        err = S.lng_error(p, m, r)[1]
+        t = time.perf_counter()
+        bs = S.surrogate_ladder(p, m, T0, T1, 32)
+        t_s = time.perf_counter() - t
+        t = time.perf_counter()
+        bl, info = S.learned_ladder(p, m, T0, T1, 32, seed=11 + i)
+        t_l = time.perf_counter() - t
+        t = time.perf_counter()
+        bm = pticm.cae_ladder(p, seed=5 + i, T0=T0, T1=T1, nt=32)
+        t_m = time.perf_counter() - t
+        a_s = S.ladder_acceptance(p, bs, steps=2000, burn_in=500, seed=7 + i)
+        a_l = S.ladder_acceptance(p, bl, steps=2000, burn_in=500, seed=7 + i)
+        a_m = S.ladder_acceptance(p, bm, steps=2000, burn_in=500, seed=7 + i)
+        rows.append(dict(n=x.n, err=err, t_s=t_s, t_l=t_l, t_m=t_m, fb=int(info.fallback), d_s=dev(a_s), d_l=dev(a_l),
+                         d_m=dev(a_m), sd_s=float(a_s.std()), sd_l=float(a_l.std()), sd_m=float(a_m.std()),
+                         len_l=len(bl), len_m=len(bm)))
+    col = lambda k: np.array([q[k] for q in rows], np.float64)
+    # time to target on a subset of held-out instances
+    ttt = []
+    cand = [i for i, x in enumerate(held) if x.n <= args.ttt_max_n][:args.ttt_count]
+    for i in cand:
+        x = held[i]
+        p = pticm.Problem.from_instance(x)
+        T0, T1 = S.pilot_range(x)
+        t = time.perf_counter()
+        bm = pticm.cae_ladder(p, seed=50 + i, T0=T0, T1=T1, nt=32)
+        t_m = time.perf_counter() - t
+        t = time.perf_counter()
+        bl, info = S.learned_ladder(p, m, T0, T1, 32, seed=60 + i)
+        t_l = time.perf_counter() - t
+        # target: best energy of a long multihistogram-laddered run, 32 copies
+        tb = pticm.Batch([p] * 32, nt=len(bm), seed=80 + i, icm=True, exchange=1)
+        tb.set_ladders(np.sort(bm))
+        tb.init_states(81 + i)
+        tb.run(args.ttt_target_steps)
+        target = float(tb.best()[0].min())
+        del tb
+        res = {"n": x.n, "name": x.name, "target": target}
+        for nm, lad, tl in (("mhist", bm, t_m), ("learned", bl, t_l)):
+            hit, msps = _ttt_runs(p, lad, target, args.ttt_copies, args.ttt_chunk, args.ttt_max_steps, 90 + i)
+            ok = hit >= 0
+            q = float(np.quantile(np.where(ok, hit, np.inf), 0.99))
+            res[nm] = {"ladder_s": tl, "temps": len(lad), "ms_per_step": msps, "success": float(ok.mean()),
+                       "steps_q99": q if np.isfinite(q) else None,
+                       "ttt99_s": (tl + q * msps / 1000.0) if np.isfinite(q) else None}
+        res["learned_fallback"] = int(info.fallback)
+        ttt.append(res)
+        log(json.dumps(res))
+    both = [t for t in ttt if t["mhist"]["ttt99_s"] and t["learned"]["ttt99_s"]]
+    speedups = [t["mhist"]["ttt99_s"] / t["learned"]["ttt99_s"] for t in both]
+    line = {
+        "metric": "time-to-target energy at 99% run success, learned vs multihistogram ladder",
+        "value": float(np.exp(np.mean(np.log(speedups)))) if speedups else None, "unit": "x (geometric mean of "
+        "multihistogram TTT99 / learned TTT99)", "higher_is_better": True, "n_gpus": 1, "data": "synthetic",
+        "dtype": "bf16 network, fp64 multihistogram", "config": {"workload": LADDER_WORKLOAD,
+        "train_instances": len(train), "held_out": len(held), "training_rows": n_rows, "generate_s": t_gen,
+        "training_data_s": t_data, "train_s": t_train, "final_loss": float(losses[-50:].mean())},
+        "lng_error_per_spin": {"mean": float(col("err").mean()), "median": float(np.median(col("err"))),
+                               "p90": float(np.quantile(col("err"), 0.9))},
+        "acceptance_mean_abs_dev": {"surrogate": float(col("d_s").mean()), "learned": float(col("d_l").mean()),
+                                    "multihistogram": float(col("d_m").mean())},
+        "acceptance_std": {"surrogate": float(col("sd_s").mean()), "learned": float(col("sd_l").mean()),
+                           "multihistogram": float(col("sd_m").mean())},
+        "fallback_rate": float(col("fb").mean()),
+        "ladder_seconds": {"surrogate_mean": float(col("t_s").mean()), "learned_mean": float(col("t_l").mean()),
+                           "learned_accepted_mean": float(col("t_l")[col("fb") == 0].mean()) if (col("fb") == 0).any() else None,
+                           "multihistogram_mean": float(col("t_m").mean())},
+        "time_to_target": ttt,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -319,9 +543,25 @@ def main():
     ap.add_argument("--cpu-pts", type=int, default=400)
     ap.add_argument("--ref-pts", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="c2", choices=["c2", "batched", "ladder"],
+                    help="c2: the headline single-instance workload; batched: 1024 uneven instances; "
+                         "ladder: the learned temperature ladder")
+    ap.add_argument("--batch-count", type=int, default=BATCH_COUNT)
+    ap.add_argument("--ladder-train", type=int, default=4096)
+    ap.add_argument("--ladder-held", type=int, default=256)
+    ap.add_argument("--ttt-count", type=int, default=8)
+    ap.add_argument("--ttt-max-n", type=int, default=500)
+    ap.add_argument("--ttt-copies", type=int, default=100)
+    ap.add_argument("--ttt-chunk", type=int, default=50)
+    ap.add_argument("--ttt-max-steps", type=int, default=10000)
+    ap.add_argument("--ttt-target-steps", type=int, default=10000)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batched":
+        return run_gpu_batched(args)
+    if args.workload == "ladder":
+        return run_gpu_ladder(args)
     return run_gpu(args)
 
 

@@ -330,6 +330,9 @@ PTICM_API int pticm_batch_enable_energy_histograms(pticm_batch* b, uint64_t from
  * be NULL to query the sizes. */
 PTICM_API int pticm_batch_get_energy_histograms(pticm_batch* b, uint32_t inst, uint32_t* hist, int64_t* e_lo,
                                                 uint64_t* nbins);
+/* The multihistogram ln g of every instance in one device launch (kept for
+ * pticm_batch_logdos until the next run). */
+PTICM_API int pticm_batch_compute_logdos(pticm_batch* b, double estep);
 /* The FP64 multihistogram ln g of one instance from its histograms
  * (temperatures merged over chains; make_histogram and get_partition_iterate,
  * src/cae_estimator.cc:45-69,228-253).  Bin k is energy min_emin + k*estep. */
@@ -359,6 +362,55 @@ PTICM_API int pticm_mlp_gradients(pticm_mlp* m, const float* x, const float* y, 
 PTICM_API int pticm_mlp_train(pticm_mlp* m, const float* x, const float* y, uint64_t n, uint32_t steps, float lr,
                               uint64_t seed, float* loss_per_step);
 PTICM_API int pticm_mlp_predict(pticm_mlp* m, const float* x, uint64_t n, float* y);
+/* Flat parameter file: "PTICMMLP", u32 version 1, u64 count, count floats. */
+PTICM_API int pticm_mlp_save(pticm_mlp* m, const char* path);
+PTICM_API int pticm_mlp_load(pticm_mlp* m, const char* path);
+
+/* ------------------------------------------------ learned temperature ladder -- */
+/* The network's instance features: ln N / 10, ln M / 12, mean degree / 20,
+ * degree std / 10, coupling mean, coupling std; its seventh input is the
+ * normalised energy x = E / W, W = sum |J| + sum |h|; its output ln g / N. */
+PTICM_API int pticm_problem_features(const pticm_problem* p, float* out6);
+/* Predicted ln g on the exact energy levels E = emin + k*estep <= 0.  The
+ * levels are those the couplings allow: estep = 2 gcd_i gcd(h_i + sum_j J_ij,
+ * 2 J_ij) (4 on +-1 lattices of even degree), in the residue class of the
+ * all-up state.  The network output y gives s = ln 2 - E^2/(2 N V) + y/10
+ * (V = sum J^2 + sum h^2), ln g = N s. */
+PTICM_API int pticm_surrogate_logdos(const pticm_problem* p, pticm_mlp* m, double* logdos, uint64_t cap,
+                                     uint64_t* nbins, double* emin, double* estep);
+/* get_beta's constant-acceptance walk (src/cae_estimator.cc:367-425) on the
+ * predicted ln g: no pilot run.  Arguments as pticm_cae_ladder. */
+PTICM_API int pticm_surrogate_ladder(const pticm_problem* p, pticm_mlp* m, double T0, double T1, int inverse,
+                                     uint32_t nt, double step_size, double r, double* beta_out, uint32_t* count);
+/* Exchange acceptance of each neighbouring pair of a ladder, measured by a
+ * PT run (two chains, no ICM) of burn_in + steps steps: acc[k], k < nt-1. */
+PTICM_API int pticm_ladder_acceptance(const pticm_problem* p, const double* beta, uint32_t nt, uint64_t seed,
+                                      uint64_t steps, uint64_t burn_in, double* acc);
+typedef struct pticm_learned_ladder_info {
+    uint32_t surrogate_count;   /* temperatures the surrogate ladder placed        */
+    int32_t fallback;           /* 1: the multihistogram ladder was used            */
+    double mean_deviation;      /* mean |acceptance - r| at the last check          */
+    uint32_t rounds;            /* acceptance checks run (1 to 3)                   */
+    uint32_t inserted;          /* temperatures the feedback placement added        */
+    double first_deviation;     /* mean |acceptance - r| of the surrogate ladder    */
+} pticm_learned_ladder_info;
+/* The surrogate ladder, checked by pticm_ladder_acceptance over check_steps
+ * steps (plus check_steps/4 burn-in).  While its mean |acceptance - r|
+ * exceeds tol (0.05), the ladder is placed again from the measured
+ * acceptances (pticm_feedback_ladder) and checked again, at most twice; if
+ * it still deviates, the multihistogram ladder of pticm_cae_ladder (2000
+ * samples, 5000 burn-in) replaces it. */
+/* Feedback placement from measured acceptances acc[k] of the gaps of a
+ * descending ladder: sigma_k = 2 erfc^-1(acc_k) / (beta_k - beta_{k+1}) (the
+ * exchange acceptance of Gaussian energy distributions of width sigma is
+ * erfc(dbeta sigma / 2)); the new ladder walks down from beta[0] with
+ * dbeta = 2 erfc^-1(r) / sigma until beta_end or nt temperatures.  attempts
+ * bounds the acceptance of a gap that saw no exchange. */
+PTICM_API int pticm_feedback_ladder(const double* beta, uint32_t count, const double* acc, double attempts, double r,
+                                    uint32_t nt, double beta_end, double* beta_out, uint32_t* out_count);
+PTICM_API int pticm_learned_ladder(const pticm_problem* p, pticm_mlp* m, double T0, double T1, int inverse,
+                                   uint32_t nt, double r, uint64_t check_steps, double tol, uint64_t seed,
+                                   double* beta_out, uint32_t* count, pticm_learned_ladder_info* info);
 
 /* ----------------------------------------------------------- utilities -- */
 PTICM_API const char* pticm_last_error(void);

@@ -15,12 +15,14 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <memory>
 #include <numeric>
 #include <random>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "pticm.h"
@@ -65,6 +67,8 @@ struct pticm_batch {
     double last_ms = 0.0;
     uint64_t hist_from = 0;
     bool hist_on = false;
+    std::vector<MhOutput> dos;           // multihistogram ln g per instance (pticm_batch_compute_logdos)
+    double dos_estep = 0.0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     DArr<InstanceDesc> d_desc;
@@ -86,6 +90,8 @@ struct pticm_batch {
 };
 
 namespace {
+
+double model_step_us(const InstanceDesc& D, int g, int threads);
 
 int batch_teams(const InstanceDesc& D, int threads) {
     const int npairs = D.nc * (D.chains / 2);
@@ -113,7 +119,9 @@ int plan_batch(pticm_batch* b, std::string& msg) {
     };
     SmemPlan S = layout_plan(dims_for(-1));
     while (S.total > kSmemLimit) {
-        // shrink the ICM teams of the instances with the largest scratch
+        // shrink the ICM teams of the instances with the largest scratch;
+        // when every instance is down to one team, split the instance with
+        // the most replica sites per block over more blocks
         uint64_t worst = 0;
         for (int i = 0; i < b->count; i++)
             worst = std::max(worst, (uint64_t)teams[i] * icm_team_bytes(Ds[i].n_pad));
@@ -124,8 +132,23 @@ int plan_batch(pticm_batch* b, std::string& msg) {
                 changed = true;
             }
         if (!changed) {
-            msg = "the replicas of one block do not fit in shared memory; raise the group of the largest instance";
-            return PTICM_ERR_UNSUPPORTED;
+            int big = -1;
+            uint64_t sites = 0;
+            for (int i = 0; i < b->count; i++) {
+                const uint64_t si = (uint64_t)Ds[i].rpc * (uint64_t)Ds[i].n_pad;
+                if (Ds[i].rpc > 1 && si > sites) { sites = si; big = i; }
+            }
+            if (big < 0) {
+                msg = "the largest instance does not fit a block even with one replica per block";
+                return PTICM_ERR_UNSUPPORTED;
+            }
+            int g = b->group[big] + 1;
+            while (b->R % g) g++;
+            b->group[big] = g;
+            Ds[big].group = g;
+            Ds[big].rpc = b->R / g;
+            teams[big] = batch_teams(Ds[big], b->threads);
+            if (!b->tuned) b->step_us[big] = model_step_us(Ds[big], g, b->threads);
         }
         S = layout_plan(dims_for(-1));
     }
@@ -542,6 +565,7 @@ int pticm_batch_run(pticm_batch* b, uint64_t pt_steps, uint32_t phase_mask) {
     if (!b->states_set) return bfail(PTICM_ERR_INVALID, "initialise the replica states before running");
     if (phase_mask == 0 || phase_mask > 7) return bfail(PTICM_ERR_INVALID, "phase_mask must be in 1..7");
     if (int rc = configure_batch(b)) return rc;
+    b->dos.clear();
     b->last_ms = 0.0;
     uint64_t left = pt_steps;
     while (left > 0) {
@@ -575,6 +599,9 @@ int pticm_batch_autotune(pticm_batch* b, uint32_t trial_steps) {
             want = 2 * g;
         }
     }
+    // measured step time per instance and group actually run (the planner
+    // may raise a group so that the batch's shared-memory plan fits)
+    std::vector<std::vector<int>> mg(b->count);
     std::vector<std::vector<double>> meas(b->count);
     const std::vector<int> keep_group = b->group;
     for (int t = 0; t < 3; t++) {
@@ -600,9 +627,24 @@ int pticm_batch_autotune(pticm_batch* b, uint32_t trial_steps) {
             worst[inst] = std::max(worst[inst], (double)ns[j] * 1e-3 / (trial_steps - 1));
         }
         for (int i = 0; i < b->count; i++)
-            if (t < (int)cand[i].size()) meas[i].push_back(worst[i]);
+            if (std::find(mg[i].begin(), mg[i].end(), b->group[i]) == mg[i].end()) {
+                mg[i].push_back(b->group[i]);
+                meas[i].push_back(worst[i]);
+            }
         if (int rc = snapshot(b, snap, false)) return rc;
     }
+    // sort each instance's measurements by group
+    for (int i = 0; i < b->count; i++) {
+        std::vector<int> ord(mg[i].size());
+        std::iota(ord.begin(), ord.end(), 0);
+        std::sort(ord.begin(), ord.end(), [&](int x, int y) { return mg[i][x] < mg[i][y]; });
+        std::vector<int> g2;
+        std::vector<double> m2;
+        for (int k : ord) { g2.push_back(mg[i][k]); m2.push_back(meas[i][k]); }
+        mg[i] = g2;
+        meas[i] = m2;
+    }
+    cand = mg;
     // choose: most efficient group (least block-time g*t) first, then split
     // the instances that are longer than the average lane load
     std::vector<int> pick(b->count);
@@ -774,20 +816,63 @@ int pticm_batch_get_energy_histograms(pticm_batch* b, uint32_t inst, uint32_t* h
     return PTICM_OK;
 }
 
+int pticm_batch_compute_logdos(pticm_batch* b, double estep) {
+    if (!b || !(estep > 0)) return bfail(PTICM_ERR_INVALID, "invalid arguments");
+    if (!b->hist_on) return bfail(PTICM_ERR_INVALID, "energy histograms are not enabled");
+    BCK(cudaStreamSynchronize(b->stream));
+    std::vector<MhInput> in(b->count);
+    std::vector<int> rc(b->count, PTICM_OK);
+    std::vector<std::string> msg(b->count);
+    std::atomic<int> next{0};
+    int dev = 0;
+    BCK(cudaGetDevice(&dev));
+    auto work = [&]() {
+        cudaSetDevice(dev);
+        std::vector<unsigned> rows;
+        for (int i = next++; i < b->count; i = next++) {
+            const InstanceDesc& D = b->desc[i];
+            rows.resize((size_t)D.R * (size_t)D.hist_nbins);
+            if (cudaMemcpy(rows.data(), b->d_hist.p + D.hist_off, rows.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess) {
+                rc[i] = PTICM_ERR_CUDA;
+                continue;
+            }
+            rc[i] = compact_slot_hist(rows.data(), D.nt, D.chains, D.hist_nbins, D.hist_lo,
+                                      b->beta.data() + (size_t)i * b->nt, estep, in[i]);
+        }
+    };
+    const int nthreads = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthreads; t++) pool.emplace_back(work);
+    for (auto& t : pool) t.join();
+    for (int i = 0; i < b->count; i++)
+        if (rc[i]) return bfail(rc[i], "instance " + std::to_string(i) + ": pilot histograms unusable");
+    std::vector<const MhInput*> ptrs;
+    for (auto& x : in) ptrs.push_back(&x);
+    if (int r = mhist_dos_multi(ptrs, b->dos)) return r;
+    b->dos_estep = estep;
+    return PTICM_OK;
+}
+
 int pticm_batch_logdos(pticm_batch* b, uint32_t inst, double estep, double* logdos, uint64_t cap, uint64_t* nbins,
                        double* min_emin, uint64_t* iterations) {
     if (!b || (int)inst >= b->count || !nbins || !(estep > 0)) return bfail(PTICM_ERR_INVALID, "invalid arguments");
     if (!b->hist_on) return bfail(PTICM_ERR_INVALID, "energy histograms are not enabled");
-    BCK(cudaStreamSynchronize(b->stream));
-    const InstanceDesc& D = b->desc[inst];
-    std::vector<unsigned> rows((size_t)D.R * (size_t)D.hist_nbins);
-    BCK(cudaMemcpy(rows.data(), b->d_hist.p + D.hist_off, rows.size() * 4, cudaMemcpyDeviceToHost));
     std::vector<double> dos, z;
     double me = 0.0;
     uint64_t it = 0;
-    if (int rc = slot_hist_dos(rows.data(), D.nt, D.chains, D.hist_nbins, D.hist_lo, b->beta.data() + (size_t)inst * b->nt,
-                               estep, dos, z, me, it))
-        return rc;
+    if (b->dos_estep == estep && (int)b->dos.size() == b->count) {
+        dos = b->dos[inst].logdos;
+        me = b->dos[inst].min_emin;
+        it = b->dos[inst].iters;
+    } else {
+        BCK(cudaStreamSynchronize(b->stream));
+        const InstanceDesc& D = b->desc[inst];
+        std::vector<unsigned> rows((size_t)D.R * (size_t)D.hist_nbins);
+        BCK(cudaMemcpy(rows.data(), b->d_hist.p + D.hist_off, rows.size() * 4, cudaMemcpyDeviceToHost));
+        if (int rc = slot_hist_dos(rows.data(), D.nt, D.chains, D.hist_nbins, D.hist_lo,
+                                   b->beta.data() + (size_t)inst * b->nt, estep, dos, z, me, it))
+            return rc;
+    }
     *nbins = dos.size();
     if (min_emin) *min_emin = me;
     if (iterations) *iterations = it;

@@ -22,6 +22,7 @@
 #include "problem_host.h"
 #include "runtime_internal.h"
 #include "mhist_host.h"
+#include "mhist_job.h"
 
 namespace pticm {
 cudaError_t launch_engine(const EngineArgs& A, int threads, bool replay, bool block_team, bool cooperative,
@@ -450,53 +451,117 @@ int reset_run_state(pticm_ctx* c) {
 }  // namespace
 
 namespace pticm {
-cudaError_t mhist_iterate(const uint32_t* hist, const uint64_t* hoff, const uint64_t* hlen, const double* emin,
-                          const double* beta, double* logZ, int nt, double estep, double min_emin, double logn,
-                          long long nbins, double* logdos, double* pmax, double* psum, int chunks, double* metric,
-                          cudaStream_t st);
+cudaError_t mhist_solve(const MhJob* jobs, int njobs, int max_nt, const uint32_t* hist, const uint64_t* hoff,
+                        const uint64_t* hlen, const double* emin, const double* beta, double* logdos, double* logc,
+                        float* ldf, double* logZ, unsigned long long* iters, long long max_iters, cudaStream_t st);
 }  // namespace pticm
 
 namespace pticm {
 
-// The multihistogram fixed point on the GPU (src/cae_estimator.cc:228-253):
-// iterate until sum_j ((lnZ_j - lnZ'_j)/lnZ'_j)^2 <= 1e-7, as the reference.
+// The multihistogram fixed point on the GPU (src/cae_estimator.cc:228-253)
+// for any number of histogram sets in one launch (mhist_solve): iterate
+// until sum_j ((lnZ_j - lnZ'_j)/lnZ'_j)^2 <= 1e-7, as the reference does.
+int mhist_dos_multi(const std::vector<const MhInput*>& in, std::vector<MhOutput>& out) {
+    const size_t K = in.size();
+    out.assign(K, MhOutput{});
+    std::vector<MhJob> jobs;
+    std::vector<uint32_t> hist;
+    std::vector<uint64_t> hoff, hlen;
+    std::vector<double> emin, beta;
+    int64_t bins = 0;
+    int max_nt = 1;
+    std::vector<size_t> solved;
+    for (size_t k = 0; k < K; k++) {
+        const MhInput& I = *in[k];
+        const uint32_t nt = (uint32_t)I.beta.size();
+        if (nt < 1 || I.n == 0 || !(I.estep > 0) || I.hoff.size() != nt || I.hlen.size() != nt || I.emin.size() != nt)
+            return fail(PTICM_ERR_INVALID, "multihistogram needs samples, rows and estep > 0");
+        double me = I.emin[0];
+        for (uint32_t j = 1; j < nt; j++) me = std::min(me, I.emin[j]);
+        const long long nb = (long long)std::ceil((I.max_emax - me) / I.estep);
+        out[k].min_emin = me;
+        out[k].logdos.assign((size_t)std::max<long long>(nb, 0), -DBL_MAX);
+        out[k].logZ.assign(nt, 0.0);
+        out[k].iters = 0;
+        if (nb <= 0) continue;
+        MhJob J{};
+        J.nt = (int32_t)nt;
+        J.row0 = (int64_t)beta.size();
+        J.nbins = nb;
+        J.bin0 = bins;
+        J.min_emin = me;
+        J.estep = I.estep;
+        J.logn = std::log((double)I.n);
+        const uint64_t base = hist.size();
+        hist.insert(hist.end(), I.hist.begin(), I.hist.end());
+        for (uint32_t j = 0; j < nt; j++) {
+            hoff.push_back(base + I.hoff[j]);
+            hlen.push_back(I.hlen[j]);
+        }
+        emin.insert(emin.end(), I.emin.begin(), I.emin.end());
+        beta.insert(beta.end(), I.beta.begin(), I.beta.end());
+        bins += nb;
+        max_nt = std::max(max_nt, (int)nt);
+        jobs.push_back(J);
+        solved.push_back(k);
+    }
+    if (jobs.empty()) return PTICM_OK;
+    DArr<MhJob> d_jobs;
+    DArr<uint32_t> d_hist;
+    DArr<uint64_t> d_off, d_len;
+    DArr<unsigned long long> d_it;
+    DArr<double> d_emin, d_beta, d_logZ, d_dos, d_logc;
+    DArr<float> d_ldf;
+    CK(d_jobs.upload(jobs));
+    CK(d_hist.upload(hist, 1));
+    CK(d_off.upload(hoff));
+    CK(d_len.upload(hlen));
+    CK(d_emin.upload(emin));
+    CK(d_beta.upload(beta));
+    CK(d_logZ.alloc(beta.size()));
+    CK(d_dos.alloc((size_t)bins));
+    CK(d_logc.alloc((size_t)bins));
+    CK(d_ldf.alloc((size_t)bins));
+    CK(d_it.alloc(jobs.size()));
+    CK(mhist_solve(d_jobs.p, (int)jobs.size(), max_nt, d_hist.p, d_off.p, d_len.p, d_emin.p, d_beta.p, d_dos.p,
+                   d_logc.p, d_ldf.p, d_logZ.p, d_it.p, kMhistMaxIters, nullptr));
+    CK(cudaDeviceSynchronize());
+    std::vector<double> dos, z;
+    std::vector<unsigned long long> it;
+    CK(d_dos.download(dos));
+    CK(d_logZ.download(z));
+    CK(d_it.download(it));
+    for (size_t q = 0; q < jobs.size(); q++) {
+        MhOutput& o = out[solved[q]];
+        std::copy(dos.begin() + jobs[q].bin0, dos.begin() + jobs[q].bin0 + jobs[q].nbins, o.logdos.begin());
+        std::copy(z.begin() + jobs[q].row0, z.begin() + jobs[q].row0 + jobs[q].nt, o.logZ.begin());
+        o.iters = it[q];
+        if (o.iters >= (uint64_t)kMhistMaxIters)
+            return fail(PTICM_ERR_DEVICE, "multihistogram fixed point did not converge within the iteration cap");
+    }
+    return PTICM_OK;
+}
+
 int mhist_dos_impl(const uint32_t* hist, const uint64_t* hoff, const uint64_t* hlen, uint32_t nt,
                    const double* beta, const double* emin, double estep, uint64_t n, double max_emax,
                    std::vector<double>& logdos, std::vector<double>& logZ, double& min_emin, uint64_t& iters) {
     if (nt < 1 || n == 0 || !(estep > 0)) return fail(PTICM_ERR_INVALID, "multihistogram needs samples, rows and estep > 0");
-    min_emin = emin[0];
-    for (uint32_t j = 1; j < nt; j++) min_emin = std::min(min_emin, emin[j]);
-    const long long nbins = (long long)std::ceil((max_emax - min_emin) / estep);
-    logdos.assign((size_t)std::max<long long>(nbins, 0), -DBL_MAX);
-    logZ.assign(nt, 0.0);
-    iters = 0;
-    if (nbins <= 0) return PTICM_OK;
+    MhInput I;
     const uint64_t total = hoff[nt - 1] + hlen[nt - 1];
-    DArr<uint32_t> d_hist;
-    DArr<uint64_t> d_off, d_len;
-    DArr<double> d_emin, d_beta, d_logZ, d_dos, d_pmax, d_psum, d_metric;
-    CK(d_hist.upload(std::vector<uint32_t>(hist, hist + total)));
-    CK(d_off.upload(std::vector<uint64_t>(hoff, hoff + nt)));
-    CK(d_len.upload(std::vector<uint64_t>(hlen, hlen + nt)));
-    CK(d_emin.upload(std::vector<double>(emin, emin + nt)));
-    CK(d_beta.upload(std::vector<double>(beta, beta + nt)));
-    CK(d_logZ.upload(logZ));
-    CK(d_dos.alloc((size_t)nbins));
-    const int chunks = (int)std::max<long long>(1, std::min<long long>(64, nbins / 2048));
-    CK(d_pmax.alloc((size_t)nt * chunks));
-    CK(d_psum.alloc((size_t)nt * chunks));
-    CK(d_metric.alloc(1));
-    const double logn = std::log((double)n);
-    for (uint64_t it = 0; it < 1000000; it++) {
-        CK(mhist_iterate(d_hist.p, d_off.p, d_len.p, d_emin.p, d_beta.p, d_logZ.p, (int)nt, estep, min_emin, logn,
-                         nbins, d_dos.p, d_pmax.p, d_psum.p, chunks, d_metric.p, nullptr));
-        double metric = 0;
-        CK(cudaMemcpy(&metric, d_metric.p, sizeof(double), cudaMemcpyDeviceToHost));
-        iters = it + 1;
-        if (!(metric > 1e-7)) break;
-    }
-    CK(d_dos.download(logdos));
-    CK(d_logZ.download(logZ));
+    I.hist.assign(hist, hist + total);
+    I.hoff.assign(hoff, hoff + nt);
+    I.hlen.assign(hlen, hlen + nt);
+    I.emin.assign(emin, emin + nt);
+    I.beta.assign(beta, beta + nt);
+    I.estep = estep;
+    I.n = n;
+    I.max_emax = max_emax;
+    std::vector<MhOutput> out;
+    if (int rc = mhist_dos_multi({&I}, out)) return rc;
+    logdos.swap(out[0].logdos);
+    logZ.swap(out[0].logZ);
+    min_emin = out[0].min_emin;
+    iters = out[0].iters;
     return PTICM_OK;
 }
 
@@ -505,12 +570,15 @@ int mhist_dos_impl(const uint32_t* hist, const uint64_t* hoff, const uint64_t* h
 // then cut to [emin_j, emax_j] with bin width estep (make_histogram,
 // src/cae_estimator.cc:45-69); n is the sample count of temperature 0,
 // accumulated into an int as the reference does.
-int slot_hist_dos(const unsigned* rows, int nt, int chains, long long nbins, long long lo, const double* hb,
-                  double estep, std::vector<double>& dos, std::vector<double>& logZ, double& min_emin,
-                  uint64_t& iters) {
-    std::vector<uint64_t> hoff(nt), hlen(nt);
-    std::vector<double> emin(nt), emax(nt);
-    std::vector<uint32_t> hist;
+int compact_slot_hist(const unsigned* rows, int nt, int chains, long long nbins, long long lo, const double* hb,
+                      double estep, MhInput& I) {
+    I = MhInput{};
+    I.hoff.resize(nt);
+    I.hlen.resize(nt);
+    I.emin.resize(nt);
+    I.beta.assign(hb, hb + nt);
+    I.estep = estep;
+    std::vector<double> emax(nt);
     std::vector<unsigned> merged((size_t)nbins);
     for (int j = 0; j < nt; j++) {
         std::fill(merged.begin(), merged.end(), 0u);
@@ -522,26 +590,38 @@ int slot_hist_dos(const unsigned* rows, int nt, int chains, long long nbins, lon
         for (long long bb = 0; bb < nbins; bb++)
             if (merged[bb]) { if (first < 0) first = bb; last = bb; }
         if (first < 0) return fail(PTICM_ERR_DEVICE, "pilot run recorded no energies");
-        emin[j] = (double)(lo + 2 * first);
+        I.emin[j] = (double)(lo + 2 * first);
         emax[j] = (double)(lo + 2 * last);
-        hlen[j] = (uint64_t)std::ceil((emax[j] - emin[j]) / estep) + 1;
-        hoff[j] = hist.size();
-        hist.resize(hist.size() + hlen[j], 0);
+        I.hlen[j] = (uint64_t)std::ceil((emax[j] - I.emin[j]) / estep) + 1;
+        I.hoff[j] = I.hist.size();
+        I.hist.resize(I.hist.size() + I.hlen[j], 0);
         for (long long bb = first; bb <= last; bb++)
-            if (merged[bb]) hist[hoff[j] + (uint64_t)std::floor(((double)(lo + 2 * bb) - emin[j]) / estep)] += merged[bb];
+            if (merged[bb]) I.hist[I.hoff[j] + (uint64_t)std::floor(((double)(lo + 2 * bb) - I.emin[j]) / estep)] += merged[bb];
     }
     int32_t nacc = 0;   // the reference accumulates row 0 into an int
-    for (uint64_t k = 0; k < hlen[0]; k++) nacc = (int32_t)(nacc + (int32_t)hist[hoff[0] + k]);
-    const double max_emax = *std::max_element(emax.begin(), emax.end());
-    return mhist_dos_impl(hist.data(), hoff.data(), hlen.data(), (uint32_t)nt, hb, emin.data(), estep,
-                          (uint64_t)(int64_t)nacc, max_emax, dos, logZ, min_emin, iters);
+    for (uint64_t k = 0; k < I.hlen[0]; k++) nacc = (int32_t)(nacc + (int32_t)I.hist[I.hoff[0] + k]);
+    I.n = (uint64_t)(int64_t)nacc;
+    I.max_emax = *std::max_element(emax.begin(), emax.end());
+    return PTICM_OK;
 }
 
-}  // namespace
+int slot_hist_dos(const unsigned* rows, int nt, int chains, long long nbins, long long lo, const double* hb,
+                  double estep, std::vector<double>& dos, std::vector<double>& logZ, double& min_emin,
+                  uint64_t& iters) {
+    MhInput I;
+    if (int rc = compact_slot_hist(rows, nt, chains, nbins, lo, hb, estep, I)) return rc;
+    std::vector<MhOutput> out;
+    if (int rc = mhist_dos_multi({&I}, out)) return rc;
+    dos.swap(out[0].logdos);
+    logZ.swap(out[0].logZ);
+    min_emin = out[0].min_emin;
+    iters = out[0].iters;
+    return PTICM_OK;
+}
 
-namespace pticm {
 const HostProblem& problem_host(const pticm_problem* p) { return p->hp; }
 void set_last_error(const std::string& m) { g_err = m; }
+
 }  // namespace pticm
 
 extern "C" {

@@ -81,6 +81,25 @@ void finish_desc(InstanceDesc& D, const HostProblem& P, const pticm_opts& o, con
 int ladder_tables(const HostProblem& P, const double* beta, int nt, int nc_req, bool icm, int chains,
                   std::vector<uint32_t>& thr, std::vector<double>& ptab);
 
+// One multihistogram input in make_histogram's layout
+// (src/cae_estimator.cc:45-69) and its solution.
+struct MhInput {
+    std::vector<uint32_t> hist;
+    std::vector<uint64_t> hoff, hlen;
+    std::vector<double> emin, beta;
+    double estep = 2.0;
+    uint64_t n = 0;
+    double max_emax = 0.0;
+};
+struct MhOutput {
+    std::vector<double> logdos, logZ;
+    double min_emin = 0.0;
+    uint64_t iters = 0;
+};
+constexpr long long kMhistMaxIters = 300000;
+int mhist_dos_multi(const std::vector<const MhInput*>& in, std::vector<MhOutput>& out);
+int compact_slot_hist(const unsigned* rows, int nt, int chains, long long nbins, long long lo, const double* hb,
+                      double estep, MhInput& I);
 int mhist_dos_impl(const uint32_t* hist, const uint64_t* hoff, const uint64_t* hlen, uint32_t nt,
                    const double* beta, const double* emin, double estep, uint64_t n, double max_emax,
                    std::vector<double>& logdos, std::vector<double>& logZ, double& min_emin, uint64_t& iters);

@@ -115,6 +115,7 @@ def lib():
         "pticm_batch_enable_energy_histograms": [P, u64],
         "pticm_batch_get_energy_histograms": [P, u32, P, P, P],
         "pticm_batch_logdos": [P, u32, dbl, P, u64, P, P, P],
+        "pticm_batch_compute_logdos": [P, dbl],
         "pticm_mlp_create": [u64, u32, C.POINTER(P)],
         "pticm_mlp_get_params": [P, P],
         "pticm_mlp_set_params": [P, P],
@@ -122,6 +123,14 @@ def lib():
         "pticm_mlp_gradients": [P, P, P, u32, P, P],
         "pticm_mlp_train": [P, P, P, u64, u32, C.c_float, u64, P],
         "pticm_mlp_predict": [P, P, u64, P],
+        "pticm_mlp_save": [P, C.c_char_p],
+        "pticm_mlp_load": [P, C.c_char_p],
+        "pticm_problem_features": [P, P],
+        "pticm_surrogate_logdos": [P, P, P, u64, P, P, P],
+        "pticm_surrogate_ladder": [P, P, dbl, dbl, C.c_int, u32, dbl, dbl, P, P],
+        "pticm_ladder_acceptance": [P, P, u32, u64, u64, u64, P],
+        "pticm_feedback_ladder": [P, u32, P, dbl, dbl, u32, dbl, P, P],
+        "pticm_learned_ladder": [P, P, dbl, dbl, C.c_int, u32, dbl, u64, dbl, u64, P, P, P],
     }
     for name, args in sigs.items():
         f = getattr(L, name)
@@ -519,6 +528,10 @@ class Batch:
         h = np.zeros((self.R, nb.value), np.uint32)
         _check(lib().pticm_batch_get_energy_histograms(self._h, inst, _p(h), C.byref(lo), C.byref(nb)))
         return h, lo.value + 2 * np.arange(nb.value)
+
+    def compute_logdos(self, estep=2.0):
+        """ln g of every instance in one device launch (cached for logdos)."""
+        _check(lib().pticm_batch_compute_logdos(self._h, estep))
 
     def logdos(self, inst, estep=2.0):
         hb = C.c_uint64()

@@ -12,6 +12,8 @@ Workload shapes:
   * ``random_graph(n, m)``  m distinct uniform pairs, weights +1 or +-1
     (C2: n=2000, m=19990, w=+1; C5: n=20000, m=400000, +-1).
   * ``batch_mix(count)``  the uneven 1024-instance mix of the batched workload.
+  * ``ladder_mix(count)``  lattices and random graphs of the learned-ladder
+    workload (training and held-out sets).
 """
 from __future__ import annotations
 
@@ -120,6 +122,24 @@ def batch_mix(count: int = 1024, seed0: int = 1000):
             n = int(round(math.exp(rng.uniform(math.log(200), math.log(5000)))))
             deg = rng.uniform(3, 20)
             m = max(1, int(round(n * deg / 2)))
+            out.append(random_graph(n, m, seed=seed0 + i, signed=True))
+    return out
+
+
+def ladder_mix(count: int, seed0: int = 5000, L_range=(6, 50), n_range=(100, 3000), deg_range=(3.0, 20.0)):
+    """Instances of the learned-ladder workload: half +-J toroidal lattices
+    with L uniform in L_range, half random +-1 graphs with n log-uniform in
+    n_range and mean degree uniform in deg_range; instance i uses seed
+    seed0 + i."""
+    out = []
+    for i in range(count):
+        rng = np.random.default_rng(seed0 + i)
+        if i % 2 == 0:
+            out.append(pm_lattice(int(rng.integers(L_range[0], L_range[1] + 1)), seed=seed0 + i))
+        else:
+            n = int(round(math.exp(rng.uniform(math.log(n_range[0]), math.log(n_range[1])))))
+            deg = rng.uniform(*deg_range)
+            m = min(n * (n - 1) // 2, max(1, int(round(n * deg / 2))))
             out.append(random_graph(n, m, seed=seed0 + i, signed=True))
     return out
 

@@ -151,7 +151,11 @@ def test_batch_logdos_matches_oracle():
     bat.init_states(14)
     bat.enable_energy_histograms(300)
     bat.run(1300)
+    single = [bat.logdos(i) for i in range(len(probs))]
+    bat.compute_logdos()   # every instance in one launch: the same numbers
     for i in range(len(probs)):
+        d_all, me_all, it_all = bat.logdos(i)
+        assert np.array_equal(d_all, single[i][0]) and me_all == single[i][1] and it_all == single[i][2]
         rows, e = bat.energy_histograms(i)
         hist, off, ln, emin, max_emax, n = _compact(rows, e, nt)
         dos_o, _, _ = O.partition_iterate(hist, off, ln, hb, emin, 2.0, n, max_emax)

@@ -303,6 +303,8 @@ typedef struct pticm_batch_info {
     double makespan_us;     /* predicted device time of one PT step of all instances */
     uint64_t pt_steps, attempts;
     double last_run_ms;
+    uint64_t launches;      /* engine launches of pticm_batch_run so far; each is sized from the measured
+                               step time to about 0.5 s (the first after a new schedule: one step) */
 } pticm_batch_info;
 PTICM_API int pticm_batch_create(const pticm_problem* const* problems, uint32_t count, const pticm_opts* o,
                                  pticm_batch** out);

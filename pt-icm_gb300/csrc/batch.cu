@@ -45,7 +45,7 @@ int bfail(int code, const std::string& m) {
         if (e_ != cudaSuccess) return bfail(PTICM_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-constexpr double kLaunchTargetUs = 250000.0;   // aim: one launch ~0.25 s, far inside the 2 s wait limit
+constexpr double kLaunchTargetUs = 500000.0;   // aim: one launch ~0.5 s, a quarter of the 2 s wait limit
 
 }  // namespace
 
@@ -61,9 +61,11 @@ struct pticm_batch {
     bool ladder_set = false, states_set = false, tuned = false;
     int lanes = 0, chunk = 1;
     double makespan_us = 0.0;            // predicted per PT step
+    double step_ms_measured = 0.0;       // device time of one PT step of the current schedule (0: unknown)
+    std::vector<int32_t> sched_measured; // the schedule step_ms_measured belongs to
     SmemPlan plan{};
     std::vector<int32_t> sched_off, sched;
-    uint64_t steps_done = 0, attempts = 0, sites_total = 0;
+    uint64_t steps_done = 0, attempts = 0, sites_total = 0, launches = 0;
     double last_ms = 0.0;
     uint64_t hist_from = 0;
     bool hist_on = false;
@@ -249,7 +251,12 @@ int configure_batch(pticm_batch* b) {
     if (gmax > b->lanes)
         return bfail(PTICM_ERR_UNSUPPORTED, "an instance needs more blocks than can be resident at once");
     b->makespan_us = build_schedule(b);
-    b->chunk = (int)std::max(1.0, std::min(65536.0, std::floor(kLaunchTargetUs / std::max(b->makespan_us, 1e-3))));
+    // launches are sized from measured step times only (the model can be far
+    // off): a schedule not measured yet starts with one-step launches
+    if (b->sched != b->sched_measured) b->step_ms_measured = 0.0;
+    b->chunk = b->step_ms_measured > 0
+                   ? (int)std::max(1.0, std::min(65536.0, std::floor(kLaunchTargetUs / 1000.0 / b->step_ms_measured)))
+                   : 1;
     for (int i = 0; i < b->count; i++) b->desc[i].first_block = 0;
     BCK(b->d_desc.upload(b->desc));
     BCK(b->d_sched_off.upload(b->sched_off));
@@ -572,6 +579,12 @@ int pticm_batch_run(pticm_batch* b, uint64_t pt_steps, uint32_t phase_mask) {
         const int chunk = (int)std::min<uint64_t>(left, (uint64_t)b->chunk);
         float ms = 0.f;
         if (int rc = batch_launch(b, b->steps_done, chunk, phase_mask, nullptr, &ms)) return rc;
+        b->launches++;
+        if (phase_mask == 7u) {
+            b->step_ms_measured = std::max((double)ms / chunk, 1e-6);
+            b->sched_measured = b->sched;
+            b->chunk = (int)std::max(1.0, std::min(65536.0, std::floor(kLaunchTargetUs / 1000.0 / b->step_ms_measured)));
+        }
         b->last_ms += ms;
         b->steps_done += (uint64_t)chunk;
         if (phase_mask & PHASE_SWEEP) b->attempts += (uint64_t)chunk * b->o.sweeps * b->sites_total;
@@ -615,16 +628,19 @@ int pticm_batch_autotune(pticm_batch* b, uint32_t trial_steps) {
         }
         DArr<unsigned long long> job_ns;
         BCK(job_ns.alloc(b->sched.size() / 2));
+        // a two-step launch sizes the trial so that it stays near the launch target
         float ms = 0.f;
-        if (int rc = batch_launch(b, b->steps_done, (int)trial_steps, PHASE_SWEEP | PHASE_EXCHANGE | PHASE_ICM,
-                                  job_ns.p, &ms))
+        if (int rc = batch_launch(b, b->steps_done, 2, PHASE_SWEEP | PHASE_EXCHANGE | PHASE_ICM, nullptr, &ms))
+            return rc;
+        const int steps_t = (int)std::max(3.0, std::min((double)trial_steps, std::floor(kLaunchTargetUs / 1000.0 / std::max(ms / 2.0, 1e-6))));
+        if (int rc = batch_launch(b, b->steps_done, steps_t, PHASE_SWEEP | PHASE_EXCHANGE | PHASE_ICM, job_ns.p, &ms))
             return rc;
         std::vector<unsigned long long> ns;
         BCK(job_ns.download(ns));
         std::vector<double> worst(b->count, 0.0);
         for (size_t j = 0; j < ns.size(); j++) {
             const int inst = b->sched[2 * j];
-            worst[inst] = std::max(worst[inst], (double)ns[j] * 1e-3 / (trial_steps - 1));
+            worst[inst] = std::max(worst[inst], (double)ns[j] * 1e-3 / (steps_t - 1));
         }
         for (int i = 0; i < b->count; i++)
             if (std::find(mg[i].begin(), mg[i].end(), b->group[i]) == mg[i].end()) {
@@ -695,6 +711,7 @@ int pticm_batch_get_info(pticm_batch* b, pticm_batch_info* info) {
     info->pt_steps = b->steps_done;
     info->attempts = b->attempts;
     info->last_run_ms = b->last_ms;
+    info->launches = b->launches;
     return PTICM_OK;
 }
 

@@ -825,8 +825,14 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
 
     int32_t* s_col = sm_ptr<int32_t>(smem, S.col);
     int32_t* s_h = sm_ptr<int32_t>(smem, S.h);
-    B.spin = sm_ptr<int8_t>(smem, S.spin);
-    B.field = sm_ptr<int32_t>(smem, S.field);
+    if (S.state_global) {
+        // replicas too large for shared memory work on their master copy
+        B.spin = A.spins + D.spin_off + (long long)B.r0 * D.n_pad;
+        B.field = A.fields + D.spin_off + (long long)B.r0 * D.n_pad;
+    } else {
+        B.spin = sm_ptr<int8_t>(smem, S.spin);
+        B.field = sm_ptr<int32_t>(smem, S.field);
+    }
     uint32_t* s_thr = sm_ptr<uint32_t>(smem, S.thr);
     double* s_ptab = sm_ptr<double>(smem, S.ptab);
     B.slot = sm_ptr<uint32_t>(smem, S.slot);
@@ -847,7 +853,7 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
     uint32_t* s_xrand = sm_ptr<uint32_t>(smem, S.xrand);
     int* s_lvl = sm_ptr<int>(smem, S.xlevel);
     uint32_t* s_tmp = sm_ptr<uint32_t>(smem, S.xpos);
-    uint8_t* s_icm = smem + S.icm;
+    uint8_t* s_icm = S.state_global ? A.icm_pool + (size_t)blockIdx.x * (size_t)A.icm_pool_stride : smem + S.icm;
     int* s_misc = sm_ptr<int>(smem, S.misc);
     long long* s_team_acc = sm_ptr<long long>(smem, S.misc + 64);
     int* s_team_bc = sm_ptr<int>(smem, S.misc + 64 + 8 * 32);   // 2 ints per team
@@ -886,7 +892,7 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
     for (int i = tid; i <= D.ncolors; i += T) s_col[i] = A.col[D.col_off + i];
     if (D.has_h)
         for (int i = tid; i < n; i += T) s_h[i] = A.hpool[D.h_off + i];
-    {
+    if (!S.state_global) {
         const long long base = D.spin_off + (long long)B.r0 * npad;
         for (int idx = tid; idx < rpc * npad; idx += T) {
             B.spin[idx] = A.spins[base + idx];
@@ -1033,7 +1039,7 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
         for (int q = 0; q < PROF_PHASES; q++) A.prof[(size_t)blockIdx.x * PROF_PHASES + q] += (unsigned long long)P.c[q];
     }
     // ---- write the block's state back
-    {
+    if (!S.state_global) {
         const long long base = D.spin_off + (long long)B.r0 * npad;
         for (int idx = tid; idx < rpc * npad; idx += T) {
             A.spins[base + idx] = B.spin[idx];

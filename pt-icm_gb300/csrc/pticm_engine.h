@@ -68,6 +68,7 @@ struct SmemPlan {
     uint32_t icm, icm_team_bytes;
     uint32_t misc;
     int32_t stage_adj;
+    int32_t state_global;       // replica spins/fields and ICM scratch in device memory (large instances)
     int32_t teams;              // ICM teams (warps, or one block-wide team)
     int32_t max_n_pad, max_kmax, max_R, max_nt;
 };
@@ -132,6 +133,8 @@ struct EngineArgs {
     unsigned long long seed;
     unsigned long long* prof;     // optional: per block, clock64 cycles per phase (PROF_PHASES)
     unsigned long long* job_ns;   // optional: per job, ns from the start of its step 1 to its end
+    uint8_t* icm_pool;            // state_global: per block ICM scratch (icm_pool_stride bytes)
+    long long icm_pool_stride;
     // optional per-slot energy histograms (the pilot run of the multihistogram
     // ladder): after the sweeps of every step >= hist_from, slot k of an
     // instance counts the energy E of its replica in bin (E - hist_lo) / 2 of

@@ -104,6 +104,8 @@ struct pticm_ctx {
     DArr<unsigned int> d_bar;
     DArr<int> d_abort;
     DArr<DevStatus> d_status;
+    DArr<uint8_t> d_icm_pool;   // ICM scratch when the replicas live in device memory
+    long long icm_stride = 0;
 
     ~pticm_ctx() {
         if (ev0) cudaEventDestroy(ev0);
@@ -153,8 +155,9 @@ SmemPlan layout_plan(const PlanDims& d) {
     }
     S.col = take((d.ncolors + 1) * 4);
     S.h = take(d.n_h * 4);
-    S.spin = take(d.spin_sites);
-    S.field = take(d.spin_sites * 4);
+    S.state_global = d.state_global ? 1 : 0;
+    S.spin = take(d.state_global ? 0 : d.spin_sites);
+    S.field = take(d.state_global ? 0 : d.spin_sites * 4);
     S.thr = take(d.nt_kst * 4);
     S.ptab = take(d.replay ? d.nt_kst * 8 : 0);
     S.slot = take(d.R * 4);
@@ -176,7 +179,7 @@ SmemPlan layout_plan(const PlanDims& d) {
     S.xpos = take(d.nt * 4);
     S.icm_team_bytes = icm_team_bytes((int32_t)d.max_n_pad);
     S.teams = d.teams;
-    S.icm = take(d.icm_bytes);
+    S.icm = take(d.state_global ? 0 : d.icm_bytes);
     S.misc = take(64 + 8 * 32 + 4 * 64 + 64);
     S.total = (uint32_t)off;
     S.max_n_pad = (int32_t)d.max_n_pad;
@@ -186,9 +189,10 @@ SmemPlan layout_plan(const PlanDims& d) {
     return S;
 }
 
-SmemPlan make_plan(const InstanceDesc& D, bool replay, int teams, int threads, bool stage_adj) {
+SmemPlan make_plan(const InstanceDesc& D, bool replay, int teams, int threads, bool stage_adj, bool state_global) {
     PlanDims d;
     d.replay = replay;
+    d.state_global = state_global;
     d.add(D, stage_adj, teams);
     (void)threads;
     return layout_plan(d);
@@ -223,7 +227,7 @@ int choose_config(const HostProblem& P, const pticm_opts& o, bool replay, Instan
         while (rpc < R && (R / rpc > sms || R % rpc != 0)) rpc++;
     }
     if (rpc <= 0 || R % rpc != 0) { msg = "replicas_per_block must divide the replica count"; return PTICM_ERR_INVALID; }
-    const int group = R / rpc;
+    int group = R / rpc;
     int threads = (int)o.block_threads;
     if (replay) threads = std::min(1024, 32 * std::max(1, std::min(R, 32)));
     if (threads <= 0) {
@@ -234,16 +238,59 @@ int choose_config(const HostProblem& P, const pticm_opts& o, bool replay, Instan
         msg = "block_threads must be a multiple of 32, at most 1024";
         return PTICM_ERR_INVALID;
     }
-    const bool block_team = (rpc == 1) && !replay;
+    bool block_team = (rpc == 1) && !replay;
     int teams = block_team ? 1 : std::max(1, std::min(threads / 32, std::max(1, npairs)));
     SmemPlan plan;
-    bool stage = true;
+    bool stage = true, global = false;
+    const int teams0 = teams;
     while (!fits(rpc, threads, teams, stage, plan)) {
         if (stage) { stage = false; continue; }
         if (teams > 1) { teams = std::max(1, teams / 2); continue; }
-        msg = "the replicas of one block do not fit in shared memory; use fewer replicas per block";
-        return PTICM_ERR_UNSUPPORTED;
+        // the replicas do not fit shared memory: keep them (and the ICM
+        // scratch) in device memory, where the 129 MB L2 holds them
+        if (replay) {
+            msg = "replay needs the replicas in shared memory; the instance is too large";
+            return PTICM_ERR_UNSUPPORTED;
+        }
+        global = true;
+        // with the state in device memory a block needs little shared
+        // memory: one replica per block (the whole block is one ICM team)
+        // when smaller blocks let all R blocks be resident at once
+        bool placed = false;
+        if (o.replicas_per_block == 0 && o.block_threads == 0) {
+            for (int t : {512, 256, 128}) {
+                InstanceDesc d1 = D;
+                d1.rpc = 1;
+                d1.group = R;
+                const SmemPlan p1 = make_plan(d1, false, 1, t, false, true);
+                if (p1.total > kSmemLimit) continue;
+                int per_sm = 0;
+                if (engine_max_blocks_per_sm(false, true, t, p1.total, &per_sm) != cudaSuccess) continue;
+                if ((int64_t)per_sm * sms < R) continue;
+                rpc = 1;
+                threads = t;
+                block_team = true;
+                teams = 1;
+                plan = p1;
+                placed = true;
+                break;
+            }
+        }
+        if (!placed) {
+            InstanceDesc t = D;
+            t.rpc = rpc;
+            t.group = R / rpc;
+            teams = block_team ? 1 : std::min(teams0, 16);
+            plan = make_plan(t, false, teams, threads, false, true);
+        }
+        if (plan.total > kSmemLimit) {
+            msg = "the per-temperature tables of the instance do not fit in shared memory";
+            return PTICM_ERR_UNSUPPORTED;
+        }
+        break;
     }
+    cfg.state_global = global;
+    group = R / rpc;
     D.rpc = rpc;
     D.group = group;
     D.teams = teams;
@@ -347,6 +394,11 @@ int configure(pticm_ctx* c, bool replay) {
     c->block_team = cfg.block_team;
     c->plan = cfg.plan;
     finish_desc(c->desc, c->P, c->o, cfg);
+    if (cfg.state_global) {
+        c->icm_stride = (long long)cfg.teams * icm_team_bytes(c->desc.n_pad);
+        const size_t want = (size_t)cfg.group * (size_t)c->icm_stride;
+        if (c->d_icm_pool.n != want) CK(c->d_icm_pool.alloc(want));
+    }
     std::vector<int32_t> soff, sched;
     single_instance_schedule(cfg.group, soff, sched);
     CK(c->d_sched_off.upload(soff));
@@ -396,6 +448,8 @@ EngineArgs make_args(pticm_ctx* c) {
     A.hist = c->d_hist.p;
     A.hist_from = c->hist_from;
     A.flags = engine_flags(c->P, c->o);
+    A.icm_pool = c->d_icm_pool.p;
+    A.icm_pool_stride = c->icm_stride;
     return A;
 }
 

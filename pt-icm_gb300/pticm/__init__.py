@@ -44,7 +44,7 @@ class BatchInfo(C.Structure):
     _fields_ = [("count", C.c_uint32), ("lanes", C.c_uint32), ("chunk", C.c_uint32), ("jobs", C.c_uint32),
                 ("smem_bytes", C.c_uint32), ("threads", C.c_uint32), ("tuned", C.c_uint32),
                 ("makespan_us", C.c_double), ("pt_steps", C.c_uint64), ("attempts", C.c_uint64),
-                ("last_run_ms", C.c_double)]
+                ("last_run_ms", C.c_double), ("launches", C.c_uint64)]
 
 
 class Stats(C.Structure):

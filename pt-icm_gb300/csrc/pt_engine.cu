@@ -258,6 +258,7 @@ __device__ void icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOC
     }
     if (threadIdx.x == 0) P.subtick(PROF_ICM_SEED);
     const int algo = D.icm_algo;
+    bool absolute = false;   // energies set from scratch (large clusters)
     if (cnt > 0 && algo != ENGINE_ICM_BFS) {
         // label the components of the whole overlap subgraph, then flip the
         // sites sharing the seed's label
@@ -317,26 +318,67 @@ __device__ void icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOC
         if (!ok) dev_fail(A.status, A.abort_flag, DEV_UF_LIMIT, where_err + 3, q, algo);
         if (threadIdx.x == 0) P.subtick(PROF_ICM_UNION);
         const int root = (algo == ENGINE_ICM_UNION_FIND) ? uf_find(vl, seed) : vl[seed];
+        // pass 1: flip the cluster's spins (marked in d as 2) and count it
+        long long csize = 0;
         for (int u = team.tr; u < n; u += team.ts) {
             if (!d[u]) continue;
             const int lu = (algo == ENGINE_ICM_UNION_FIND) ? uf_find(vl, u) : vl[u];
             if (lu != root) continue;
+            d[u] = 2;
+            csize++;
             const int hu = D.has_h ? B.h[u] : 0;
-            int sa = 0, sb = 0;
-            if (locA) { sa = sA[u]; sA[u] = (int8_t)-sa; dEa -= 2 * sa * hu; }
-            if (locB) { sb = sB[u]; sB[u] = (int8_t)-sb; dEb -= 2 * sb * hu; }
-            const int e1 = B.row[u + 1];
+            if (locA) { const int sa = sA[u]; sA[u] = (int8_t)-sa; dEa -= 2 * sa * hu; }
+            if (locB) { const int sb = sB[u]; sB[u] = (int8_t)-sb; dEb -= 2 * sb * hu; }
+        }
+        {
+            unsigned long long m1 = ~0ull, m2 = ~0ull;
+            long long none = 0;
+            team.reduce(csize, m1, m2, none);
+        }
+        if (BLOCK && csize * 4 > (long long)n) {
+            // a large cluster: fields and energies from scratch (gathers, no
+            // atomics; the cost does not grow with the cluster)
+            long long eA = 0, eB = 0;
+            for (int i = team.tr; i < n; i += team.ts) {
+                int fa = 0, fb = 0;
+                const int e1 = B.row[i + 1];
 #pragma unroll 4
-            for (int a = B.row[u]; a < e1; a++) {
-                const uint32_t e = B.adj[a];
-                const int v = (int)(e >> 8);
-                const int J = (int)(int8_t)(e & 0xffu);
-                if (locA) atomicAdd(fA + v, J * (-2 * sa));
-                if (locB) atomicAdd(fB + v, J * (-2 * sb));
-                if (!d[v]) {
-                    const int sv = locA ? sA[v] : sB[v];
-                    if (locA) dEa -= 2 * J * sa * sv;
-                    if (locB) dEb -= 2 * J * sb * sv;
+                for (int a = B.row[i]; a < e1; a++) {
+                    const uint32_t e = B.adj[a];
+                    const int v = (int)(e >> 8);
+                    const int J = (int)(int8_t)(e & 0xffu);
+                    if (locA) fa += J * sA[v];
+                    if (locB) fb += J * sB[v];
+                }
+                const int h2 = D.has_h ? 2 * B.h[i] : 0;
+                if (locA) { fA[i] = fa; eA += (long long)sA[i] * (h2 + fa); }
+                if (locB) { fB[i] = fb; eB += (long long)sB[i] * (h2 + fb); }
+            }
+            team.sum2(eA, eB);
+            if (team.tr == 0) {
+                if (locA) B.E[rA] = eA / 2;
+                if (locB) B.E[rB] = eB / 2;
+            }
+            absolute = true;
+        } else {
+            // a small cluster: push the field changes to the neighbours and
+            // take the energy change from the edges leaving the cluster
+            for (int u = team.tr; u < n; u += team.ts) {
+                if (d[u] != 2) continue;
+                const int sa = locA ? -sA[u] : 0, sb = locB ? -sB[u] : 0;   // spins before the flip
+                const int e1 = B.row[u + 1];
+#pragma unroll 4
+                for (int a = B.row[u]; a < e1; a++) {
+                    const uint32_t e = B.adj[a];
+                    const int v = (int)(e >> 8);
+                    const int J = (int)(int8_t)(e & 0xffu);
+                    if (locA) atomicAdd(fA + v, J * (-2 * sa));
+                    if (locB) atomicAdd(fB + v, J * (-2 * sb));
+                    if (!d[v]) {
+                        const int sv = locA ? sA[v] : sB[v];
+                        if (locA) dEa -= 2 * J * sa * sv;
+                        if (locB) dEb -= 2 * J * sb * sv;
+                    }
                 }
             }
         }
@@ -404,7 +446,7 @@ __device__ void icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOC
         }
         if (threadIdx.x == 0) P.subtick(PROF_ICM_UNION);
     }
-    if (gflip || cnt > 0) {
+    if (!absolute && (gflip || cnt > 0)) {
         team.sum2(dEa, dEb);
         if (team.tr == 0) {
             if (locA) B.E[rA] += dEa;

@@ -38,7 +38,9 @@ void usage() {
         "  --replicas-per-block N      replicas held by one thread block (default automatic)\n"
         "  --threads N                 threads per block (default automatic)\n"
         "  --icm-algo auto|bfs|union-find|label-prop\n"
-        "  --sort-ladder               sort a --preprocess ladder ascending (ICM on the coldest)\n");
+        "  --sort-ladder               sort a --preprocess or learned ladder ascending (ICM on the coldest)\n"
+        "  --learned-ladder FILE       constant-acceptance ladder from a trained surrogate network (no pilot\n"
+        "                              run); checked by a short PT run, multihistogram ladder as fallback\n");
 }
 
 }  // namespace
@@ -89,6 +91,7 @@ int main(int argc, char** argv) {
                 else if (v == "label-prop") P.icm_algo = 3;
                 else throw std::runtime_error("unknown --icm-algo " + v);
             } else if (a == "--sort-ladder") P.sort_ladder = true;
+            else if (a == "--learned-ladder") P.learned_ladder = next();
             else throw std::runtime_error("unknown argument " + a);
         }
         if (!help && problem_path.empty()) throw std::runtime_error("--problem is required");

@@ -45,6 +45,7 @@ struct Parameters {
     uint32_t block_threads = 0;       // 0 automatic
     uint32_t icm_algo = 0;            // 0 automatic, 1 BFS, 2 union-find, 3 label propagation
     bool sort_ladder = false;         // sort a --preprocess ladder ascending (ICM on the coldest)
+    std::string learned_ladder;       // surrogate network file: learned ladder (multihistogram fallback)
 };
 
 // include/problem.hh:7-98

@@ -1,5 +1,6 @@
 // shim.cc -- the reference's C++ interface over the GB300 engine's C ABI.
 #include <algorithm>
+#include <memory>
 #include <charconv>
 #include <chrono>
 #include <cstdio>
@@ -108,9 +109,32 @@ void get_beta(PTWorker& w, double estep, double step_size, double r, size_t num_
     w.beta_values = beta;
 }
 
+// The learned ladder: the surrogate network's constant-acceptance ladder,
+// checked by a short PT run, with the multihistogram ladder as fallback.
+void learned_beta(PTWorker& w, double r) {
+    pticm_mlp* m = nullptr;
+    check(pticm_mlp_create(w.params.seed, 1024, &m));
+    std::unique_ptr<pticm_mlp, void (*)(pticm_mlp*)> hold(m, pticm_mlp_destroy);
+    check(pticm_mlp_load(m, w.params.learned_ladder.c_str()));
+    std::vector<double> beta(w.params.Nt);
+    uint32_t count = 0;
+    pticm_learned_ladder_info info{};
+    check(pticm_learned_ladder(w.p.handle(), m, w.params.T0, w.params.T1, w.params.inverse ? 1 : 0,
+                               (uint32_t)w.params.Nt, r, 1000, 0.05, w.params.seed, beta.data(), &count, &info));
+    beta.resize(count);
+    w.params.Nt = count;
+    w.beta_values = beta;
+    if (w.params.verbosity)
+        std::printf("learned ladder: %u temperatures, %s (mean |acceptance - r| %.3f after %u checks)\n", count,
+                    info.fallback ? "multihistogram fallback" : "accepted", info.mean_deviation, info.rounds);
+}
+
 void initialize_temperatures(PTWorker& w) {
     w.characteristic_scale = w.p.get_char_scale();
-    if (w.params.preprocess) {
+    if (!w.params.learned_ladder.empty()) {
+        learned_beta(w, 0.4);
+        if (w.params.sort_ladder) std::sort(w.beta_values.begin(), w.beta_values.end());
+    } else if (w.params.preprocess) {
         get_beta(w, 2, w.params.pre_step, 0.4, w.params.pre_samples);
         if (w.params.sort_ladder) std::sort(w.beta_values.begin(), w.beta_values.end());
     } else {

@@ -86,3 +86,25 @@ def test_saved_network_predicts_the_same(trained):
         S.save(m, path)
         m2 = S.load(path)
     assert np.array_equal(S.surrogate_logdos(p, m2)[0], d0)
+
+
+def test_cli_learned_ladder(trained):
+    """pt_icm --learned-ladder: the ladder comes from the saved network (or
+    its multihistogram fallback) and the run reports as usual."""
+    import re
+    import subprocess
+    from pticm import surrogate as S
+    m, _, _, _ = trained
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cli = os.path.join(root, "pt-icm_gb300", "bin", "pt_icm")
+    graph = os.path.join(root, "tests", "golden", "graphs", "pmL20_c1.gset")
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "net.bin")
+        S.save(m, path)
+        out = subprocess.run([cli, "-p", graph, "-s", "3", "-r", "24", "--pts", "2000", "--icm", "-T0", "0.5",
+                              "-T1", "3.0", "--learned-ladder", path, "--sort-ladder", "--verbose", "1"],
+                             capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    m_l = re.search(r"learned ladder: (\d+) temperatures, (accepted|multihistogram fallback)", out.stdout)
+    assert m_l and int(m_l.group(1)) >= 2
+    assert re.search(r"^best_energy: -?[0-9.]+", out.stdout, re.M)

@@ -268,12 +268,57 @@ __device__ void icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOC
         for (int i = team.tr; i < n; i += team.ts) lab[i] = d[i] ? i : n;
         team.sync();
         if (algo == ENGINE_ICM_UNION_FIND) {
+            // Afforest (Sutton, Ben-Nun, Barak, IPDPS 2018): link every
+            // overlap site to its first two overlap neighbours, compress,
+            // take the most frequent root of a sample as the large component
+            // L, then process the full adjacency only of sites outside L.  An
+            // edge skipped at an end in L is processed from its other end,
+            // unless that end is in L too -- then both are already joined.
             for (int u = team.tr; u < n; u += team.ts) {
                 if (!d[u]) continue;
+                int k = 0;
                 const int e1 = B.row[u + 1];
+                for (int a = B.row[u]; a < e1 && k < 2; a++) {
+                    const int v = (int)(B.adj[a] >> 8);
+                    if (d[v]) {
+                        ok &= uf_unite(lab, u, v);
+                        k++;
+                    }
+                }
+            }
+            team.sync();
+            for (int u = team.tr; u < n; u += team.ts) {
+                if (!d[u]) continue;
+                const int r = uf_find(vl, u);
+                if (r < 0) ok = false;
+                else vl[u] = r;
+            }
+            team.sync();
+            if (team.tr < 32) {
+                // vote over 32 sampled overlap sites (one warp)
+                int cand = -1;
+                const int i0 = (int)(((long long)team.tr * n) >> 5);
+                for (int t = 0; t < 32 && i0 + t < n; t++)
+                    if (d[i0 + t]) { cand = vl[i0 + t]; break; }
+                const unsigned grp = __match_any_sync(0xffffffffu, cand);
+                int votes = cand >= 0 ? __popc(grp) : 0, best = cand;
+                for (int o = 16; o > 0; o >>= 1) {
+                    const int ov = __shfl_xor_sync(0xffffffffu, votes, o);
+                    const int oc = __shfl_xor_sync(0xffffffffu, best, o);
+                    if (ov > votes || (ov == votes && oc < best)) { votes = ov; best = oc; }
+                }
+                if (team.tr == 0) team.ctl[0] = best;
+            }
+            team.sync();
+            const int L = *(volatile int*)team.ctl;
+            for (int u = team.tr; u < n; u += team.ts) {
+                if (!d[u]) continue;
+                if (uf_find(vl, u) == L) continue;
+                const int e1 = B.row[u + 1];
+#pragma unroll 4
                 for (int a = B.row[u]; a < e1; a++) {
                     const int v = (int)(B.adj[a] >> 8);
-                    if (v > u && d[v]) ok &= uf_unite(lab, u, v);
+                    if (d[v]) ok &= uf_unite(lab, u, v);
                 }
             }
             team.sync();
@@ -289,9 +334,11 @@ __device__ void icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOC
                     const int lu = vl[u];
                     int best = lu;
                     const int e1 = B.row[u + 1];
+#pragma unroll 4
                     for (int a = B.row[u]; a < e1; a++) {
                         const int v = (int)(B.adj[a] >> 8);
-                        if (d[v]) best = min(best, vl[v]);
+                        const int lv = vl[v];
+                        if (d[v]) best = min(best, lv);
                     }
                     if (best < lu) {
                         atomicMin(lab + lu, best);
@@ -1043,15 +1090,22 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
         if (icm_on) {
             // pairs q = cp*nc + kk: slots (2cp)*nt + k and (2cp+1)*nt + k, k = nt-1-kk
             const int npairs = D.nc * (D.chains / 2);
+            // the block's pairs, found from its own replicas' slots: replica
+            // j at slot s (chain c = s / nt, temperature k = s % nt) is in pair
+            // q = (c / 2) nc + (nt-1-k) when nt-1-k < nc; a pair with both
+            // replicas in the block is taken from its first chain's side
+            (void)npairs;
+            const int chains_even = D.chains & ~1;
             if (BLOCKTEAM) {
                 Team<true> team{tid, T, s_team_acc, s_team_bc};
                 const IcmScratch X = icm_scratch(s_icm, npad);
-                for (int q = 0; q < npairs; q++) {
-                    const int cp = q / D.nc, kk = q - cp * D.nc, k = nt - 1 - kk;
+                for (int j = 0; j < rpc; j++) {
+                    const int sl = (int)B.rslot[j], c = sl / nt, k = sl - c * nt, kk = nt - 1 - k;
+                    if (kk >= D.nc || c >= chains_even) continue;
+                    const int cp = c >> 1;
                     const int rA = (int)B.slot[(2 * cp) * nt + k], rB = (int)B.slot[(2 * cp + 1) * nt + k];
-                    const bool mine = (rA >= B.r0 && rA < B.r0 + rpc) || (rB >= B.r0 && rB < B.r0 + rpc);
-                    if (!mine) continue;
-                    icm_pair<true, REPLAY>(A, B, team, q, rA, rB, step, ls, X, 30, P);
+                    if ((c & 1) && rA >= B.r0 && rA < B.r0 + rpc) continue;
+                    icm_pair<true, REPLAY>(A, B, team, cp * D.nc + kk, rA, rB, step, ls, X, 30, P);
                 }
             } else {
                 const int warp = tid >> 5, lane = tid & 31;
@@ -1060,13 +1114,14 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
                     Team<false> team{lane, 32, s_team_acc + warp, s_team_bc + 2 * warp};
                     const IcmScratch X = icm_scratch(s_icm + (size_t)warp * icm_team_bytes(npad), npad);
                     int e = 0;
-                    for (int q = 0; q < npairs; q++) {
-                        const int cp = q / D.nc, kk = q - cp * D.nc, k = nt - 1 - kk;
+                    for (int j = 0; j < rpc; j++) {
+                        const int sl = (int)B.rslot[j], c = sl / nt, k = sl - c * nt, kk = nt - 1 - k;
+                        if (kk >= D.nc || c >= chains_even) continue;
+                        const int cp = c >> 1;
                         const int rA = (int)B.slot[(2 * cp) * nt + k], rB = (int)B.slot[(2 * cp + 1) * nt + k];
-                        const bool mine = (rA >= B.r0 && rA < B.r0 + rpc) || (rB >= B.r0 && rB < B.r0 + rpc);
-                        if (!mine) continue;
+                        if ((c & 1) && rA >= B.r0 && rA < B.r0 + rpc) continue;
                         if ((e++ % teams) != warp) continue;
-                        icm_pair<false, REPLAY>(A, B, team, q, rA, rB, step, ls, X, 30, P);
+                        icm_pair<false, REPLAY>(A, B, team, cp * D.nc + kk, rA, rB, step, ls, X, 30, P);
                     }
                 }
             }

@@ -314,11 +314,11 @@ int choose_config(const HostProblem& P, const pticm_opts& o, bool replay, Instan
 }
 
 // Engine flags for the options: exchange order, best tracking, cluster search
-// (automatic: label propagation on denser graphs, where overlap clusters are
-// large and shallow; union-find on sparse ones).
+// (automatic: union-find with Afforest sampling, the fastest measured on
+// sparse and dense graphs alike; BFS and label propagation on request).
 int engine_flags(const HostProblem& P, const pticm_opts& o) {
-    const double mean_deg = P.n ? (double)P.dadj.size() / (double)P.n : 0.0;
-    int algo = mean_deg >= 8.0 ? ENGINE_ICM_LABEL_PROP : ENGINE_ICM_UNION_FIND;
+    (void)P;
+    int algo = ENGINE_ICM_UNION_FIND;
     if (o.icm_algo == 1) algo = ENGINE_ICM_BFS;
     else if (o.icm_algo == 2) algo = ENGINE_ICM_UNION_FIND;
     else if (o.icm_algo == 3) algo = ENGINE_ICM_LABEL_PROP;

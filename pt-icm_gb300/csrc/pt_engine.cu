@@ -175,7 +175,7 @@ __device__ __forceinline__ IcmScratch icm_scratch(uint8_t* base, int n_pad) {
 // exact integer update.  Members held by another block are read from the
 // published copy and flipped by their own block, which grows the same set.
 template <bool BLOCK, bool REPLAY>
-__device__ void icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK>& team, int q,
+__device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK>& team, int q,
                          int rA, int rB, unsigned long long step, int ls, const IcmScratch& X,
                          int where_err, Prof& P) {
     const InstanceDesc& D = B.D;
@@ -236,29 +236,30 @@ __device__ void icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOC
         const long long traced = (idx < (long long)A.replay.n_icm) ? A.replay.icm_seed[idx] : -2;
         if ((traced < 0) != (cnt == 0)) {
             if (team.tr == 0) dev_fail(A.status, A.abort_flag, DEV_REPLAY_MISMATCH, where_err, idx, cnt);
-            return;
+            return 0;
         }
         if (cnt > 0) {
             if (traced >= n) {
                 if (team.tr == 0) dev_fail(A.status, A.abort_flag, DEV_BAD_INDEX, where_err + 1, idx, traced);
-                return;
+                return 0;
             }
             seed = A.perm[D.perm_off + traced];
             if (!d[seed]) {
                 if (team.tr == 0) dev_fail(A.status, A.abort_flag, DEV_REPLAY_MISMATCH, where_err + 2, idx, seed);
-                return;
+                return 0;
             }
         }
     } else if (cnt > 0) {
         seed = (int)((gflip ? ke : kd) & 0xFFFFFFFFull);
         if (seed < 0 || seed >= n) {
             if (team.tr == 0) dev_fail(A.status, A.abort_flag, DEV_BAD_INDEX, where_err + 4, q, seed);
-            return;
+            return 0;
         }
     }
     if (threadIdx.x == 0) P.subtick(PROF_ICM_SEED);
     const int algo = D.icm_algo;
-    bool absolute = false;   // energies set from scratch (large clusters)
+    bool absolute = false;   // energies set from scratch (large flipped sets)
+    int swapped = 0;         // the flipped set was D\C (the chains hold each other's result)
     if (cnt > 0 && algo != ENGINE_ICM_BFS) {
         // label the components of the whole overlap subgraph, then flip the
         // sites sharing the seed's label
@@ -365,7 +366,7 @@ __device__ void icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOC
         if (!ok) dev_fail(A.status, A.abort_flag, DEV_UF_LIMIT, where_err + 3, q, algo);
         if (threadIdx.x == 0) P.subtick(PROF_ICM_UNION);
         const int root = (algo == ENGINE_ICM_UNION_FIND) ? uf_find(vl, seed) : vl[seed];
-        // pass 1: flip the cluster's spins (marked in d as 2) and count it
+        // mark the cluster C (d = 2) and count it
         long long csize = 0;
         for (int u = team.tr; u < n; u += team.ts) {
             if (!d[u]) continue;
@@ -373,16 +374,30 @@ __device__ void icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOC
             if (lu != root) continue;
             d[u] = 2;
             csize++;
-            const int hu = D.has_h ? B.h[u] : 0;
-            if (locA) { const int sa = sA[u]; sA[u] = (int8_t)-sa; dEa -= 2 * sa * hu; }
-            if (locB) { const int sb = sB[u]; sB[u] = (int8_t)-sb; dEb -= 2 * sb * hu; }
         }
         {
             unsigned long long m1 = ~0ull, m2 = ~0ull;
             long long none = 0;
             team.reduce(csize, m1, m2, none);
         }
-        if (BLOCK && csize * 4 > (long long)n) {
+        // (A, B) -> (A flipped on C, B flipped on C) is the same pair of
+        // states as (B flipped on D\C, A flipped on D\C): flip the smaller of
+        // C and D\C.  With D\C the pair's two chains hold each other's
+        // result at this temperature -- the ICM move followed by an exchange
+        // of the two chains' configurations at one temperature, which leaves
+        // the joint distribution of the (independent, identical) chains
+        // invariant.  Replay keeps the reference's flips.
+        swapped = (!REPLAY && csize * 2 > cnt) ? 1 : 0;
+        const uint8_t fmark = swapped ? 1 : 2;
+        const long long fsize = swapped ? cnt - csize : csize;
+        for (int u = team.tr; u < n; u += team.ts) {
+            if (d[u] != fmark) continue;
+            const int hu = D.has_h ? B.h[u] : 0;
+            if (locA) { const int sa = sA[u]; sA[u] = (int8_t)-sa; dEa -= 2 * sa * hu; }
+            if (locB) { const int sb = sB[u]; sB[u] = (int8_t)-sb; dEb -= 2 * sb * hu; }
+        }
+        team.sync();
+        if (BLOCK && fsize * 4 > (long long)n) {
             // a large cluster: fields and energies from scratch (gathers, no
             // atomics; the cost does not grow with the cluster)
             long long eA = 0, eB = 0;
@@ -411,7 +426,7 @@ __device__ void icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOC
             // a small cluster: push the field changes to the neighbours and
             // take the energy change from the edges leaving the cluster
             for (int u = team.tr; u < n; u += team.ts) {
-                if (d[u] != 2) continue;
+                if (d[u] != fmark) continue;
                 const int sa = locA ? -sA[u] : 0, sb = locB ? -sB[u] : 0;   // spins before the flip
                 const int e1 = B.row[u + 1];
 #pragma unroll 4
@@ -502,6 +517,7 @@ __device__ void icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOC
     }
     team.sync();
     if (threadIdx.x == 0) P.subtick(PROF_ICM_FLIP);
+    return swapped;
 }
 
 // --------------------------------------------------------------- sweeps

@@ -106,7 +106,14 @@ def test_fields_exact_after_every_phase(pticm, g, T0, T1, nt, rpb):
     assert sorted(s2r.tolist()) == list(range(2 * nt))
     for r in range(2 * nt):
         assert s2r[slot[r]] == r
-        assert (slot[r] >= nt) == (r >= nt)      # exchange never mixes chains
+    # exchange alone never moves a replica to the other chain
+    ctx2 = pticm.Context(prob, nt=nt, seed=8, icm=True, replicas_per_block=rpb)
+    ctx2.set_ladder(pticm.beta_linspace(T0, T1, nt))
+    ctx2.init_states(12)
+    ctx2.run(40, pticm.PHASE_SWEEP | pticm.PHASE_EXCHANGE)
+    slot2 = ctx2.replicas()[3]
+    for r in range(2 * nt):
+        assert (slot2[r] >= nt) == (r >= nt)
 
 
 def _golden_runs():

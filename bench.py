@@ -128,6 +128,24 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# ------------------------------------------------------ replicas-only N>1
+def max_over_ranks(value, dist=None, device="cpu"):
+    """The largest of every rank's value (the job ends with its slowest
+    rank); the value itself on one rank."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world, units_per_rank, max_ms):
+    """Whole-job throughput of `world` independent replicas that each did
+    units_per_rank units, the job taking the slowest rank's time."""
+    return world * units_per_rank / (max_ms / 1000.0)
+
+
 # ---------------------------------------------------------------- CPU legs
 def _cpu_sample(args):
     """One oracle solve on a bounded sample of the workload (worker)."""
@@ -238,12 +256,8 @@ def run_gpu(args):
             dev_ms.append(st.last_run_ms)
     barrier()
     wall = time.perf_counter() - wall0
-    total_ms = sum(dev_ms)
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * attempts_per_step * args.steps / (total_ms / 1000.0)
+    total_ms = max_over_ranks(sum(dev_ms), dist, "cuda")
+    value = job_throughput(world, attempts_per_step * args.steps, total_ms)
     mism = ctx.verify()
 
     # end-to-end through the C ABI from host buffers, per step

@@ -191,6 +191,14 @@ PTICM_API int pticm_enable_energy_histograms(pticm_ctx* c, uint64_t from_step);
  * nbins and e_lo first. */
 PTICM_API int pticm_get_energy_histograms(pticm_ctx* c, uint32_t* hist, int64_t* e_lo, uint64_t* nbins);
 
+/* The observables of the reference's --log (src/main.cc:490-530, there
+ * commented out) from the samples collected since pticm_enable_energy_
+ * histograms' from_step, per temperature j < nt (chains merged): T = 1/beta,
+ * C = beta^2 Var(E) / N, X = beta Var(M) / N, u = <E>/N, m = <M>/N with
+ * M = sum_i s_i; samples = sample count.  Any output may be NULL. */
+PTICM_API int pticm_get_observables(pticm_ctx* c, double* T, double* C, double* X, double* u, double* m,
+                                    uint64_t* samples);
+
 /* -------------------------------------------- multihistogram ladder -- */
 /* get_beta (src/cae_estimator.cc:295-428) on the GPU: a pilot PT run
  * (gather_samples, :76-151: one chain of nt temperatures linear in beta from

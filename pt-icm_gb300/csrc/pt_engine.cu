@@ -960,6 +960,7 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
     uint32_t* s_tmp = sm_ptr<uint32_t>(smem, S.xpos);
     uint8_t* s_icm = S.state_global ? A.icm_pool + (size_t)blockIdx.x * (size_t)A.icm_pool_stride : smem + S.icm;
     int* s_misc = sm_ptr<int>(smem, S.misc);
+    long long* s_mag = sm_ptr<long long>(smem, S.mag);
     long long* s_team_acc = sm_ptr<long long>(smem, S.misc + 64);
     int* s_team_bc = sm_ptr<int>(smem, S.misc + 64 + 8 * 32);   // 2 ints per team
 
@@ -1068,6 +1069,21 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
             }
         }
         P.tick(PROF_SWEEP);
+        const bool observe = A.obs != nullptr && D.hist_nbins > 0 && step >= A.hist_from;
+        if (observe) {
+            // magnetisation of the block's replicas, one warp per replica
+            const int warp = tid >> 5, lane = tid & 31;
+            for (int j = warp; j < rpc; j += (T >> 5)) {
+                long long m = 0;
+                for (int i = lane; i < n; i += 32) m += B.spin[(long long)j * npad + i];
+                for (int o = 16; o > 0; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
+                if (lane == 0) s_mag[j] = m;
+            }
+            __syncthreads();
+            if (D.group > 1)
+                for (int j = tid; j < rpc; j += T)
+                    A.mag_pub[parity * A.energy_pub_half + D.rep_off + B.r0 + j] = s_mag[j];
+        }
         if (D.group > 1) {
             // publish this block's energies (and spins, for ICM partners)
             for (int j = tid; j < rpc; j += T) A.energy_pub[parity * A.energy_pub_half + D.rep_off + B.r0 + j] = B.E[B.r0 + j];
@@ -1083,9 +1099,18 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
         P.tick(PROF_BARRIER);
         if (A.hist != nullptr && D.hist_nbins > 0 && step >= A.hist_from && B.rank == 0) {
             for (int k = tid; k < R; k += T) {
-                const long long bin = (B.E[B.slot[k]] - D.hist_lo) >> 1;
+                const int r = (int)B.slot[k];
+                const long long bin = (B.E[r] - D.hist_lo) >> 1;
                 if (bin >= 0 && bin < D.hist_nbins)
                     atomicAdd(A.hist + D.hist_off + (long long)k * D.hist_nbins + bin, 1u);
+                if (observe) {
+                    const long long m = (r >= B.r0 && r < B.r0 + rpc)
+                                            ? s_mag[r - B.r0]
+                                            : ld_cg(A.mag_pub + parity * A.energy_pub_half + D.rep_off + r);
+                    unsigned long long* o = reinterpret_cast<unsigned long long*>(A.obs + 2 * (D.rep_off + k));
+                    atomicAdd(o, (unsigned long long)m);
+                    atomicAdd(o + 1, (unsigned long long)(m * m));
+                }
             }
             __syncthreads();
         }

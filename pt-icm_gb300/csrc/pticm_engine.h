@@ -66,6 +66,7 @@ struct SmemPlan {
     uint32_t att, succ;
     uint32_t xlogu, xrand, xlevel, xpos;
     uint32_t icm, icm_team_bytes;
+    uint32_t mag;               // rpc magnetisations (observables)
     uint32_t misc;
     int32_t stage_adj;
     int32_t state_global;       // replica spins/fields and ICM scratch in device memory (large instances)
@@ -141,6 +142,11 @@ struct EngineArgs {
     // its row k (InstanceDesc::hist_*)
     unsigned int* hist;
     unsigned long long hist_from;
+    // optional magnetisation observables (with the histograms): per slot
+    // sum of M = sum_i s_i and of M^2 at obs[2 (rep_off + slot)], and the
+    // published M of every replica (two parity halves, like energy_pub)
+    long long* obs;
+    long long* mag_pub;
     SmemPlan sm;
     ReplayArgs replay;
 };

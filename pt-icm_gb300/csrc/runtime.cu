@@ -99,6 +99,7 @@ struct pticm_ctx {
     DArr<unsigned long long> d_flips, d_bestSweep, d_att, d_succ, d_mismatch, d_prof;
     bool profiling = false;
     DArr<unsigned int> d_hist;   // pilot energy histograms (multihistogram ladder)
+    DArr<long long> d_obs, d_mag_pub;   // magnetisation sums per slot, published magnetisations
     long long hist_lo = 0, hist_nbins = 0;
     uint64_t hist_from = 0;
     DArr<unsigned int> d_bar;
@@ -180,6 +181,7 @@ SmemPlan layout_plan(const PlanDims& d) {
     S.icm_team_bytes = icm_team_bytes((int32_t)d.max_n_pad);
     S.teams = d.teams;
     S.icm = take(d.state_global ? 0 : d.icm_bytes);
+    S.mag = take(d.rpc * 8);
     S.misc = take(64 + 8 * 32 + 4 * 64 + 64);
     S.total = (uint32_t)off;
     S.max_n_pad = (int32_t)d.max_n_pad;
@@ -446,6 +448,8 @@ EngineArgs make_args(pticm_ctx* c) {
     A.sm = c->plan;
     A.prof = (c->profiling && c->d_prof.n >= (size_t)c->group * PROF_PHASES) ? c->d_prof.p : nullptr;
     A.hist = c->d_hist.p;
+    A.obs = c->d_hist.p ? c->d_obs.p : nullptr;
+    A.mag_pub = c->d_mag_pub.p;
     A.hist_from = c->hist_from;
     A.flags = engine_flags(c->P, c->o);
     A.icm_pool = c->d_icm_pool.p;
@@ -1130,6 +1134,45 @@ int pticm_enable_energy_histograms(pticm_ctx* c, uint64_t from_step) {
     c->desc.hist_lo = c->hist_lo;
     c->desc.hist_nbins = c->hist_nbins;
     CK(c->d_hist.alloc((size_t)c->R * (size_t)c->hist_nbins));
+    CK(c->d_obs.alloc(2 * (size_t)c->R));
+    CK(c->d_mag_pub.alloc(2 * (size_t)c->R));
+    return PTICM_OK;
+}
+
+int pticm_get_observables(pticm_ctx* c, double* T, double* C, double* X, double* u, double* m, uint64_t* samples) {
+    if (!c) return fail(PTICM_ERR_INVALID, "null argument");
+    if (!c->d_hist.p) return fail(PTICM_ERR_INVALID, "energy histograms are not enabled");
+    CK(cudaStreamSynchronize(c->stream));
+    std::vector<unsigned> h;
+    std::vector<long long> o;
+    CK(c->d_hist.download(h));
+    CK(c->d_obs.download(o));
+    const double n = (double)c->P.n;
+    for (int j = 0; j < c->nt; j++) {
+        double cnt = 0, se = 0, se2 = 0, sm = 0, sm2 = 0;
+        for (int ch = 0; ch < c->C; ch++) {
+            const int k = ch * c->nt + j;
+            const unsigned* row = h.data() + (size_t)k * (size_t)c->hist_nbins;
+            for (long long b = 0; b < c->hist_nbins; b++) {
+                if (!row[b]) continue;
+                const double E = (double)(c->hist_lo + 2 * b);
+                cnt += row[b];
+                se += row[b] * E;
+                se2 += row[b] * E * E;
+            }
+            sm += (double)o[2 * k];
+            sm2 += (double)o[2 * k + 1];
+        }
+        const double beta = c->beta.empty() ? 0.0 : c->beta[j];
+        const double eA = cnt > 0 ? se / cnt : 0.0, e2 = cnt > 0 ? se2 / cnt : 0.0;
+        const double mA = cnt > 0 ? sm / cnt : 0.0, m2 = cnt > 0 ? sm2 / cnt : 0.0;
+        if (T) T[j] = beta != 0.0 ? 1.0 / beta : 0.0;
+        if (C) C[j] = beta * beta * (e2 - eA * eA) / n;
+        if (X) X[j] = beta * (m2 - mA * mA) / n;
+        if (u) u[j] = eA / n;
+        if (m) m[j] = mA / n;
+        if (samples) samples[j] = (uint64_t)cnt;
+    }
     return PTICM_OK;
 }
 

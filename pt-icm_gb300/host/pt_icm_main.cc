@@ -28,7 +28,7 @@ void usage() {
         "  -T1, --temp1 X              last temperature (default 2.8)\n"
         "  -i, --inverse               T0/T1 are inverse temperatures\n"
         "  --preprocess                multihistogram constant-acceptance ladder\n"
-        "  --log                       accepted for compatibility (no effect, as in the reference)\n"
+        "  --log                       print T,C,X,u,m per temperature from the steps after burn-in\n"
         "  --icm                       isoenergetic cluster moves\n"
         "  --verbose N                 verbosity\n"
         "GPU engine options:\n"

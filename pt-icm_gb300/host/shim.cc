@@ -208,6 +208,8 @@ void solve(PTWorker& w, std::string& problem_path, double& best_ene, size_t& fli
     w.p = Problem(problem_path, w.params.seed, w.params.burn_in);
     initialize_temperatures(w);
     initialize_replicas(w);
+    // --log: per-temperature observables from the steps after the burn-in
+    if (w.params.log_data) check(pticm_enable_energy_histograms(w.ctx, w.params.burn_in));
     check(pticm_run(w.ctx, w.params.pts, PTICM_PHASE_ALL));
     size_t best_sweep = 0;
     gather_best_energy_values(w, best_ene, best_sweep, best_state);
@@ -252,6 +254,15 @@ void solve(PTWorker& w, std::string& problem_path, double& best_ene, size_t& fli
     std::printf("%s]\n", lad.c_str());
     std::printf("Total time: %.6f\n", elapsed);
     std::fflush(stdout);
+    if (w.params.log_data) {
+        // the table the reference's --log was to write (src/main.cc:490-530): T,C,X,u,m
+        const size_t nt = (size_t)w.params.Nt;
+        std::vector<double> T(nt), C(nt), X(nt), U(nt), M(nt);
+        std::vector<uint64_t> ns(nt);
+        check(pticm_get_observables(w.ctx, T.data(), C.data(), X.data(), U.data(), M.data(), ns.data()));
+        std::printf("T,C,X,u,m\n");
+        for (size_t k = 0; k < nt; k++) std::printf("%f,%f,%f,%f,%f\n", T[k], C[k], X[k], U[k], M[k]);
+    }
 }
 
 }  // namespace pticm

@@ -99,6 +99,7 @@ def lib():
         "pticm_mhist_dos": [P, P, P, u32, P, P, dbl, u64, dbl, P, u64, P, P, P],
         "pticm_cae_walk": [P, u64, dbl, dbl, dbl, dbl, dbl, dbl, u32, P, P],
         "pticm_get_profile": [P, P, P],
+        "pticm_get_observables": [P, P, P, P, P, P, P],
         "pticm_tc_gemm_check": [C.c_int, C.c_int, C.c_int, P, P, P, C.c_int, P],
         "pticm_batch_create": [P, u32, C.POINTER(Opts), C.POINTER(P)],
         "pticm_batch_set_ladders": [P, P, u32, i32],
@@ -348,6 +349,14 @@ class Context:
 
     def enable_energy_histograms(self, from_step=0):
         _check(lib().pticm_enable_energy_histograms(self._h, from_step))
+
+    def observables(self):
+        """Per temperature (chains merged): T, C, X, u, m and the sample count
+        (the table of the reference's --log)."""
+        out = [np.zeros(self.nt) for _ in range(5)]
+        n = np.zeros(self.nt, np.uint64)
+        _check(lib().pticm_get_observables(self._h, *[_p(a) for a in out], _p(n)))
+        return (*out, n)
 
     def energy_histograms(self):
         """(histograms [R, nbins], energies of the bins [nbins])."""

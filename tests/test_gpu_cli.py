@@ -56,3 +56,18 @@ def test_cli_preprocess_ladder():
     ladder = [float(x) for x in lines[-1][1:-1].split(",")]
     assert ladder[0] == pytest.approx(1 / 0.6, rel=1e-6)
     assert all(a > b for a, b in zip(ladder, ladder[1:]))
+
+
+def test_cli_log_prints_observables():
+    """--log: the T,C,X,u,m table of the reference's legacy logging, one row per
+    temperature, from the steps after the burn-in."""
+    path = os.path.join(G, "pmL10.gset")
+    text = _run("-p", path, "-s", "2", "-r", "8", "--pts", "3000", "-b", "500", "--icm", "-T0", "0.5", "-T1", "3.0",
+                "--log")
+    lines = text.splitlines()
+    i = lines.index("T,C,X,u,m")
+    rows = [[float(x) for x in l.split(",")] for l in lines[i + 1:i + 9]]
+    assert len(rows) == 8
+    for T, C, X, u, m in rows:
+        assert 0.5 - 1e-9 <= T <= 3.0 + 1e-9
+        assert C >= 0 and X >= 0 and -2.0 <= u <= 0.0 and abs(m) <= 1.0

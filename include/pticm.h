@@ -294,6 +294,10 @@ PTICM_API int pticm_run_noalloc(const pticm_problem* p, const pticm_opts* o, con
  * the surrogate network's GEMM against a reference. */
 PTICM_API int pticm_tc_gemm_check(int M, int N, int K, const uint16_t* A, const uint16_t* B, const float* bias,
                                   int act, float* C);
+/* Device time of the tensor-core GEMM at M x N x K (bf16 operands and
+ * output, FP32 accumulation), averaged over `iters` back-to-back launches
+ * after one warm-up; tflops = 2 M N K / time. */
+PTICM_API int pticm_tc_gemm_bench(int M, int N, int K, int iters, double* ms_per_gemm, double* tflops);
 
 /* ------------------------------------------------------------ batching -- */
 /* Many instances (problems of any sizes, same nt and chains) in one
@@ -400,15 +404,16 @@ typedef struct pticm_learned_ladder_info {
     uint32_t surrogate_count;   /* temperatures the surrogate ladder placed        */
     int32_t fallback;           /* 1: the multihistogram ladder was used            */
     double mean_deviation;      /* mean |acceptance - r| at the last check          */
-    uint32_t rounds;            /* acceptance checks run (1 to 3)                   */
+    uint32_t rounds;            /* acceptance checks run (1 to 4)                   */
     uint32_t inserted;          /* temperatures the feedback placement added        */
     double first_deviation;     /* mean |acceptance - r| of the surrogate ladder    */
 } pticm_learned_ladder_info;
 /* The surrogate ladder, checked by pticm_ladder_acceptance over check_steps
  * steps (plus check_steps/4 burn-in).  While its mean |acceptance - r|
  * exceeds tol (0.05), the ladder is placed again from the measured
- * acceptances (pticm_feedback_ladder) and checked again, at most twice; if
- * it still deviates, the multihistogram ladder of pticm_cae_ladder (2000
+ * acceptances (pticm_feedback_ladder) and checked again, at most three
+ * times (not at all when the first check is off by more than 0.2); if it
+ * still deviates, the multihistogram ladder of pticm_cae_ladder (2000
  * samples, 5000 burn-in) replaces it. */
 /* Feedback placement from measured acceptances acc[k] of the gaps of a
  * descending ladder: sigma_k = 2 erfc^-1(acc_k) / (beta_k - beta_{k+1}) (the

@@ -74,6 +74,53 @@ extern "C" int pticm_tc_gemm_check(int M, int N, int K, const uint16_t* A, const
     return rc;
 }
 
+extern "C" int pticm_tc_gemm_bench(int M, int N, int K, int iters, double* ms_per_gemm, double* tflops) {
+    if (M <= 0 || N <= 0 || K <= 0 || (K % 64) || iters <= 0 || !ms_per_gemm)
+        return mlp_fail(PTICM_ERR_INVALID, "need positive M, N, iters and K a multiple of 64");
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+        return mlp_fail(PTICM_ERR_NODEVICE, "no CUDA device is available");
+    __nv_bfloat16 *dA = nullptr, *dB = nullptr, *dC = nullptr;
+    DevStatus* ds = nullptr;
+    int* dab = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto cleanup = [&]() {
+        cudaFree(dA); cudaFree(dB); cudaFree(dC); cudaFree(ds); cudaFree(dab);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    };
+    if (cudaMalloc(&dA, (size_t)M * K * 2) || cudaMalloc(&dB, (size_t)N * K * 2) || cudaMalloc(&dC, (size_t)M * N * 2) ||
+        cudaMalloc(&ds, sizeof(DevStatus)) || cudaMalloc(&dab, 4)) {
+        cleanup();
+        return mlp_fail(PTICM_ERR_NOMEM, "device allocation failed");
+    }
+    cudaMemset(dA, 0x3c, (size_t)M * K * 2);   // bf16 ~1.0 everywhere: finite sums
+    cudaMemset(dB, 0x3c, (size_t)N * K * 2);
+    cudaMemset(ds, 0, sizeof(DevStatus));
+    cudaMemset(dab, 0, 4);
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaError_t e = tc_gemm(dA, dB, M, N, K, nullptr, 0, nullptr, dC, N, ds, dab, nullptr);   // warm-up
+    if (e == cudaSuccess) e = cudaEventRecord(e0, nullptr);
+    for (int i = 0; i < iters && e == cudaSuccess; i++)
+        e = tc_gemm(dA, dB, M, N, K, nullptr, 0, nullptr, dC, N, ds, dab, nullptr);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, nullptr);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    DevStatus hs{};
+    if (e == cudaSuccess) e = cudaMemcpy(&hs, ds, sizeof hs, cudaMemcpyDeviceToHost);
+    int rc = PTICM_OK;
+    if (e != cudaSuccess) rc = mlp_fail(PTICM_ERR_CUDA, std::string("tc_gemm: ") + cudaGetErrorString(e));
+    else if (hs.error) rc = mlp_fail(PTICM_ERR_DEVICE, "tc_gemm: tensor-core wait expired");
+    else {
+        *ms_per_gemm = (double)ms / iters;
+        if (tflops) *tflops = 2.0 * M * N * (double)K / (*ms_per_gemm * 1e-3) / 1e12;
+    }
+    cleanup();
+    return rc;
+}
+
 // ===================================================================== MLP
 namespace {
 

@@ -9,8 +9,9 @@
 // pilot then measures the exchange acceptance of the placed ladder; when it
 // deviates from the target by more than the tolerance (mean over pairs),
 // the ladder is placed again from the measured acceptances (feedback_ladder)
-// and measured again, at most twice; if it still deviates, the
-// multihistogram ladder (pticm_cae_ladder) is used instead.
+// and measured again, at most three times (none when the first check is off
+// by more than 0.2); if it still deviates, the multihistogram ladder
+// (pticm_cae_ladder) is used instead.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -37,7 +38,8 @@ int sfail(int code, const std::string& m) {
 
 constexpr int kFeatures = 6;
 constexpr double kTargetScale = 10.0;
-constexpr int kChecks = 3;   // acceptance checks of a learned ladder: the surrogate's, then two feedback placements
+constexpr int kChecks = 4;   // acceptance checks of a learned ladder: the surrogate's, then up to three feedback placements
+constexpr double kHopeless = 0.2;   // a first check this far off goes straight to the multihistogram ladder
 constexpr char kMagic[8] = {'P', 'T', 'I', 'C', 'M', 'M', 'L', 'P'};
 
 // ln N / 10, ln M / 12, mean degree / 20, degree std / 10, coupling mean and
@@ -299,6 +301,7 @@ int pticm_learned_ladder(const pticm_problem* p, pticm_mlp* m, double T0, double
         li.rounds = round + 1;
         if (round == 0) li.first_deviation = li.mean_deviation;
         if (li.mean_deviation <= tol || round == kChecks - 1) break;
+        if (round == 0 && li.mean_deviation > kHopeless) break;
         // feedback re-placement from the measured acceptances
         std::vector<double> out = feedback_ladder(lad, acc, (double)check_steps, r, nt, be);
         li.inserted += (uint32_t)(out.size() > lad.size() ? out.size() - lad.size() : 0);

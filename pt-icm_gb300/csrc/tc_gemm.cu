@@ -3,15 +3,17 @@
 //
 //   C[M x N] = act(A[M x K] . B[N x K]^T + bias[N])      (A, B bf16, K-major)
 //
-// One CTA of 128 threads computes a 128 x 128 tile.  Operand tiles of
-// 128 x 64 are staged in shared memory in the canonical K-major layout
-// without swizzle: 8-row x 16-byte core matrices, K-adjacent core matrices
-// 128 B apart (leading byte offset), 8-row groups 1024 B apart (stride byte
-// offset).  Thread 0 issues tcgen05.mma.kind::f16 (M=128, N=128, K=16 each,
-// FP32 accumulation) into a tensor-memory accumulator and commits to an
-// mbarrier; the four warps then read their 32 accumulator lanes with
-// tcgen05.ld and apply the epilogue (bias, optional SiLU, FP32 and/or BF16
-// stores).  Every wait is bounded; a timeout is recorded in a status word.
+// One CTA of 128 threads computes a 128 x BN tile (BN = 128, or 256 when
+// N > 128).  K advances in chunks of 64 through two shared-memory staging
+// buffers in the canonical K-major layout without swizzle: 8-row x 16-byte
+// core matrices, K-adjacent core matrices 128 B apart (leading byte offset),
+// 8-row groups 1024 B apart (stride byte offset).  Thread 0 issues
+// tcgen05.mma.kind::f16 (M=128, N=BN, K=16 each, FP32 accumulation) into a
+// tensor-memory accumulator and commits each chunk to its buffer's mbarrier;
+// the threads stage the next chunk meanwhile.  The four warps then read
+// their 32 accumulator lanes with tcgen05.ld and apply the epilogue (bias,
+// optional SiLU, FP32 and/or BF16 stores).  Every wait is bounded; a timeout
+// is recorded in a status word.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -21,9 +23,8 @@
 
 namespace pticm {
 
-constexpr int TC_BM = 128, TC_BN = 128, TC_BK = 64;
-constexpr uint32_t TC_TILE_BYTES = TC_BM * TC_BK * 2;   // 16 KB per operand tile
-constexpr uint32_t TC_TMEM_COLS = 256;                   // allocation (128 used)
+constexpr int TC_BM = 128, TC_BK = 64;
+constexpr uint32_t TC_TMEM_COLS = 256;                   // FP32 accumulator columns (N <= 256)
 
 enum TcAct : int { TC_ACT_NONE = 0, TC_ACT_SILU = 1 };
 
@@ -48,36 +49,46 @@ __device__ __forceinline__ void tc_fence_proxy_async() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-// Copy one 128 x 64 bf16 tile (rows r0.., columns k0..) of a K-major matrix
-// into the core-matrix layout; thread t moves row t.
+// Copy a tile of `nrows` x 64 bf16 (rows r0.., columns k0..) of a K-major
+// matrix into the core-matrix layout (8-row x 16-byte core matrices, K-
+// adjacent ones 128 B apart, 8-row groups 1024 B apart); thread t moves rows
+// t, t+128, ...; rows past `rows` are zero.
 __device__ __forceinline__ void tc_stage_tile(uint8_t* dst, const __nv_bfloat16* src, long long ld, int r0, int k0,
-                                              int rows) {
-    const int m = threadIdx.x;
-    uint4 v[8];
-    if (r0 + m < rows) {
-        const uint4* p = reinterpret_cast<const uint4*>(src + (long long)(r0 + m) * ld + k0);
+                                              int rows, int nrows) {
+    for (int m = threadIdx.x; m < nrows; m += blockDim.x) {
+        uint4 v[8];
+        if (r0 + m < rows) {
+            const uint4* p = reinterpret_cast<const uint4*>(src + (long long)(r0 + m) * ld + k0);
 #pragma unroll
-        for (int c = 0; c < 8; c++) v[c] = p[c];
-    } else {
+            for (int c = 0; c < 8; c++) v[c] = __ldg(p + c);
+        } else {
 #pragma unroll
-        for (int c = 0; c < 8; c++) v[c] = make_uint4(0, 0, 0, 0);
+            for (int c = 0; c < 8; c++) v[c] = make_uint4(0, 0, 0, 0);
+        }
+        uint8_t* base = dst + (m >> 3) * 1024 + (m & 7) * 16;
+#pragma unroll
+        for (int c = 0; c < 8; c++) *reinterpret_cast<uint4*>(base + c * 128) = v[c];
     }
-    uint8_t* base = dst + (m >> 3) * 1024 + (m & 7) * 16;
-#pragma unroll
-    for (int c = 0; c < 8; c++) *reinterpret_cast<uint4*>(base + c * 128) = v[c];
 }
 
+// One CTA computes a 128 x BN tile.  K advances in chunks of 64 through two
+// staging buffers: while the tensor cores run chunk k (issued by thread 0,
+// committed to that buffer's mbarrier), the threads stage chunk k+1 into
+// the other buffer, which they reuse only after the commit of chunk k-1 has
+// arrived.  Each mbarrier thus has at most one phase outstanding.
+template <int BN>
 __global__ void __launch_bounds__(128, 1)
 tc_gemm_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restrict__ B, int M, int N, int K,
                const float* __restrict__ bias, int act, float* __restrict__ Cf, __nv_bfloat16* __restrict__ Cb,
                long long ldc, DevStatus* status, int* abort_flag) {
+    constexpr uint32_t A_BYTES = TC_BM * TC_BK * 2;
+    constexpr uint32_t STAGE = A_BYTES + BN * TC_BK * 2;
     extern __shared__ __align__(1024) uint8_t tc_smem[];
-    uint8_t* sA = tc_smem;
-    uint8_t* sB = tc_smem + TC_TILE_BYTES;
-    __shared__ uint64_t mbar;
+    __shared__ uint64_t mbar[2];
     __shared__ uint32_t tmem_base_s;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * TC_BM, n0 = blockIdx.y * TC_BN;
+    const int m0 = blockIdx.x * TC_BM, n0 = blockIdx.y * BN;
+    uint8_t* buf0 = tc_smem;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_s)),
@@ -85,28 +96,33 @@ tc_gemm_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restr
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    if (threadIdx.x == 0) mbar_init(&mbar, 1);
+    if (threadIdx.x == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+    }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base_s;
+    const uint32_t idesc = tc_idesc_bf16(TC_BM, BN);
+    const int nk = K / TC_BK;
+    uint32_t ph[2] = {0u, 0u};
 
-    const uint32_t idesc = tc_idesc_bf16(TC_BM, TC_BN);
-    const uint32_t aaddr = smem_u32(sA), baddr = smem_u32(sB);
-    uint32_t phase = 0;
+    tc_stage_tile(buf0, A, K, m0, 0, M, TC_BM);
+    tc_stage_tile(buf0 + A_BYTES, B, K, n0, 0, N, BN);
+    tc_fence_proxy_async();
+    __syncthreads();
     bool ok = true;
-    for (int k0 = 0; k0 < K; k0 += TC_BK) {
-        tc_stage_tile(sA, A, K, m0, k0, M);
-        tc_stage_tile(sB, B, K, n0, k0, N);
-        tc_fence_proxy_async();
-        __syncthreads();
+    for (int kc = 0; kc < nk; kc++) {
+        const int b = kc & 1;
         if (threadIdx.x == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t aaddr = smem_u32(buf0 + b * STAGE), baddr = aaddr + A_BYTES;
 #pragma unroll
             for (int kk = 0; kk < TC_BK / 16; kk++) {
                 const uint64_t da = tc_smem_desc(aaddr + kk * 256, 128, 1024);
                 const uint64_t db = tc_smem_desc(baddr + kk * 256, 128, 1024);
-                const uint32_t accumulate = (k0 > 0 || kk > 0) ? 1u : 0u;
+                const uint32_t accumulate = (kc > 0 || kk > 0) ? 1u : 0u;
                 asm volatile(
                     "{\n\t.reg .pred p;\n\t"
                     "setp.ne.b32 p, %4, 0;\n\t"
@@ -115,19 +131,42 @@ tc_gemm_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restr
                     : "memory");
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             smem_u32(&mbar))
+                             smem_u32(&mbar[b]))
                          : "memory");
         }
-        // the tiles may be overwritten only after the MMAs have read them
-        if (!mbar_wait_bounded(&mbar, phase)) ok = false;
-        phase ^= 1u;
-        if (!ok) break;
+        if (kc + 1 < nk) {
+            const int nb = b ^ 1;
+            bool w = true;
+            if (kc >= 1) {   // the other buffer was read by the MMAs of chunk kc-1
+                w = mbar_wait_bounded(&mbar[nb], ph[nb]);
+                ph[nb] ^= 1u;
+            }
+            if (w) {
+                uint8_t* dst = buf0 + nb * STAGE;
+                tc_stage_tile(dst, A, K, m0, (kc + 1) * TC_BK, M, TC_BM);
+                tc_stage_tile(dst + A_BYTES, B, K, n0, (kc + 1) * TC_BK, N, BN);
+            }
+            tc_fence_proxy_async();
+            ok = __syncthreads_and(w) != 0;
+            if (!ok) break;
+        }
     }
+    // drain: the commits of the last two chunks not yet waited for
+    if (ok) {
+        if (nk >= 2) {
+            const int b2 = (nk - 2) & 1;
+            ok = mbar_wait_bounded(&mbar[b2], ph[b2]);
+            ph[b2] ^= 1u;
+        }
+        const int b1 = (nk - 1) & 1;
+        ok = mbar_wait_bounded(&mbar[b1], ph[b1]) && ok;
+    }
+    ok = __syncthreads_and(ok) != 0;
     if (!ok) {
-        // record the failure, then give the MMAs in flight one more bounded
-        // wait before the accumulator is released
+        // record the failure; give the MMAs in flight one more bounded wait
+        // before the accumulator is released
         if (threadIdx.x == 0 && status) dev_fail(status, abort_flag, DEV_TMA_TIMEOUT, 100, blockIdx.x, blockIdx.y);
-        mbar_wait_bounded(&mbar, phase ^ 1u);
+        mbar_wait_bounded(&mbar[(nk - 1) & 1], ph[(nk - 1) & 1]);
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
@@ -135,7 +174,7 @@ tc_gemm_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restr
     const int row = m0 + warp * 32 + lane;
     if (ok) {
 #pragma unroll 1
-        for (int c0 = 0; c0 < TC_BN; c0 += 32) {
+        for (int c0 = 0; c0 < BN; c0 += 32) {
             uint32_t r[32];
             const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
             asm volatile(
@@ -169,14 +208,23 @@ tc_gemm_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restr
 
 // Launch: M, N multiples of 128 not required (rows/cols beyond are masked),
 // K a multiple of 64 and both operands 16-byte aligned with row stride K.
+// N > 128 uses 128 x 256 tiles (one CTA covers a 256-wide layer).
 cudaError_t tc_gemm(const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N, int K, const float* bias, int act,
                     float* Cf, __nv_bfloat16* Cb, long long ldc, DevStatus* status, int* abort_flag,
                     cudaStream_t st) {
-    const size_t smem = 2 * TC_TILE_BYTES + 1024;
-    cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (N > 128) {
+        const size_t smem = 2 * (size_t)(TC_BM * TC_BK * 2 + 256 * TC_BK * 2) + 1024;
+        cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        dim3 grid((M + TC_BM - 1) / TC_BM, (N + 255) / 256);
+        tc_gemm_kernel<256><<<grid, 128, smem, st>>>(A, B, M, N, K, bias, act, Cf, Cb, ldc, status, abort_flag);
+        return cudaGetLastError();
+    }
+    const size_t smem = 2 * (size_t)(TC_BM * TC_BK * 2 + 128 * TC_BK * 2) + 1024;
+    cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    dim3 grid((M + TC_BM - 1) / TC_BM, (N + TC_BN - 1) / TC_BN);
-    tc_gemm_kernel<<<grid, 128, smem, st>>>(A, B, M, N, K, bias, act, Cf, Cb, ldc, status, abort_flag);
+    dim3 grid((M + TC_BM - 1) / TC_BM, (N + 127) / 128);
+    tc_gemm_kernel<128><<<grid, 128, smem, st>>>(A, B, M, N, K, bias, act, Cf, Cb, ldc, status, abort_flag);
     return cudaGetLastError();
 }
 

@@ -15,7 +15,8 @@ def _bf16_bits(x):
 
 
 @pytest.mark.parametrize("M,N,K,act", [(128, 128, 64, 0), (256, 256, 256, 0), (384, 128, 128, 1),
-                                       (200, 72, 64, 1), (1024, 256, 256, 1)])
+                                       (200, 72, 64, 1), (1024, 256, 256, 1), (256, 200, 512, 1),
+                                       (130, 300, 192, 0), (512, 128, 1024, 0)])
 def test_tc_gemm_matches_torch_fp32(M, N, K, act):
     torch = pytest.importorskip("torch")
     import pticm
@@ -36,3 +37,13 @@ def test_tc_gemm_matches_torch_fp32(M, N, K, act):
         assert np.allclose(pre, pre)   # finite
         ref = ref  # act applies only to the bf16 output; the fp32 output is pre-activation
     assert np.allclose(out, ref, rtol=1e-4, atol=1e-3), np.abs(out - ref).max()
+
+
+def test_tc_gemm_bench_runs():
+    import ctypes as C
+    import pticm
+    L = pticm.lib()
+    L.pticm_tc_gemm_bench.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    ms, tf = C.c_double(), C.c_double()
+    assert L.pticm_tc_gemm_bench(4096, 256, 256, 5, C.byref(ms), C.byref(tf)) == 0
+    assert ms.value > 0 and tf.value > 0

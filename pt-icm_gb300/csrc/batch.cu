@@ -95,7 +95,12 @@ namespace {
 
 double model_step_us(const InstanceDesc& D, int g, int threads);
 
+// ICM teams of an instance's blocks: one warp per pair for small instances,
+// one block-wide team (pairs in sequence) from kBlockTeamSites sites on.
+constexpr int kBlockTeamSites = 768;
+
 int batch_teams(const InstanceDesc& D, int threads) {
+    if (D.n_pad >= kBlockTeamSites) return 1;
     const int npairs = D.nc * (D.chains / 2);
     return std::max(1, std::min(threads / 32, std::max(1, npairs)));
 }

@@ -1137,7 +1137,10 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
             // replicas in the block is taken from its first chain's side
             (void)npairs;
             const int chains_even = D.chains & ~1;
-            if (BLOCKTEAM) {
+            // the whole block is one team when it holds one replica, or when
+            // the instance is configured with one team (large instances: a
+            // pair per block-wide team, in sequence, beats a pair per warp)
+            if (BLOCKTEAM || D.teams == 1) {
                 Team<true> team{tid, T, s_team_acc, s_team_bc};
                 const IcmScratch X = icm_scratch(s_icm, npad);
                 for (int j = 0; j < rpc; j++) {

@@ -241,7 +241,9 @@ int choose_config(const HostProblem& P, const pticm_opts& o, bool replay, Instan
         return PTICM_ERR_INVALID;
     }
     bool block_team = (rpc == 1) && !replay;
-    int teams = block_team ? 1 : std::max(1, std::min(threads / 32, std::max(1, npairs)));
+    // ICM teams: one warp per pair on small instances; from 768 sites on the
+    // whole block is one team (pairs in sequence), which is faster per pair
+    int teams = (block_team || D.n_pad >= 768) ? 1 : std::max(1, std::min(threads / 32, std::max(1, npairs)));
     SmemPlan plan;
     bool stage = true, global = false;
     const int teams0 = teams;

@@ -123,7 +123,7 @@ extern "C" int pticm_run_noalloc(const pticm_problem* p, const pticm_opts* o, co
     LaunchConfig cfg;
     std::string msg;
     if (int rc = choose_config(P, *o, false, D, cfg, msg)) return noalloc_fail(rc, msg);
-    if (cfg.state_global)
+    if (cfg.state_global || cfg.field_gather)
         return noalloc_fail(PTICM_ERR_UNSUPPORTED, "the replicas do not fit shared memory; use pticm_create/pticm_run");
     finish_desc(D, P, *o, cfg);
 

@@ -187,8 +187,9 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
     const int8_t* pubB = A.spins_pub + parity * A.spins_pub_half + D.spin_off + (long long)rB * npad;
     int8_t* sA = locA ? B.spin + (rA - B.r0) * npad : nullptr;
     int8_t* sB = locB ? B.spin + (rB - B.r0) * npad : nullptr;
-    int32_t* fA = locA ? B.field + (rA - B.r0) * npad : nullptr;
-    int32_t* fB = locB ? B.field + (rB - B.r0) * npad : nullptr;
+    // no stored fields in field_gather mode: field updates are skipped
+    int32_t* fA = (locA && B.field) ? B.field + (rA - B.r0) * npad : nullptr;
+    int32_t* fB = (locB && B.field) ? B.field + (rB - B.r0) * npad : nullptr;
     uint8_t* d = X.d;
     const int nwords = (n + 31) >> 5;
     if (threadIdx.x == 0) P.subtick(PROF_ICM_ENERGY);
@@ -222,7 +223,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
     long long dEa = 0, dEb = 0;
     if (gflip) {
         for (int i = team.tr; i < n; i += team.ts) {
-            if (locA) { sA[i] = (int8_t)-sA[i]; fA[i] = -fA[i]; }
+            if (locA) { sA[i] = (int8_t)-sA[i]; if (fA) fA[i] = -fA[i]; }
             d[i] ^= 1;
         }
         cnt = n - cnt;
@@ -413,8 +414,8 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                     if (locB) fb += J * sB[v];
                 }
                 const int h2 = D.has_h ? 2 * B.h[i] : 0;
-                if (locA) { fA[i] = fa; eA += (long long)sA[i] * (h2 + fa); }
-                if (locB) { fB[i] = fb; eB += (long long)sB[i] * (h2 + fb); }
+                if (locA) { if (fA) fA[i] = fa; eA += (long long)sA[i] * (h2 + fa); }
+                if (locB) { if (fB) fB[i] = fb; eB += (long long)sB[i] * (h2 + fb); }
             }
             team.sum2(eA, eB);
             if (team.tr == 0) {
@@ -434,8 +435,8 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                     const uint32_t e = B.adj[a];
                     const int v = (int)(e >> 8);
                     const int J = (int)(int8_t)(e & 0xffu);
-                    if (locA) atomicAdd(fA + v, J * (-2 * sa));
-                    if (locB) atomicAdd(fB + v, J * (-2 * sb));
+                    if (fA) atomicAdd(fA + v, J * (-2 * sa));
+                    if (fB) atomicAdd(fB + v, J * (-2 * sb));
                     if (!d[v]) {
                         const int sv = locA ? sA[v] : sB[v];
                         if (locA) dEa -= 2 * J * sa * sv;
@@ -480,8 +481,8 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                         const uint32_t e = B.adj[e0 + k];
                         v = (int)(e >> 8);
                         const int J = (int)(int8_t)(e & 0xffu);
-                        if (locA) atomicAdd(fA + v, J * (-2 * sa));
-                        if (locB) atomicAdd(fB + v, J * (-2 * sb));
+                        if (fA) atomicAdd(fA + v, J * (-2 * sa));
+                        if (fB) atomicAdd(fB + v, J * (-2 * sb));
                         if (d[v]) {
                             const uint32_t bit = 1u << (v & 31);
                             found = !(atomicOr(X.vis + (v >> 5), bit) & bit);
@@ -520,6 +521,19 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
     return swapped;
 }
 
+// Local field of site i gathered from the neighbours' spins (field_gather
+// mode, where fields are not stored): f_i = sum_j J_ij s_j.
+__device__ __forceinline__ int gather_field(const int32_t* row, const uint32_t* adj, const int8_t* sp, int i) {
+    int f = 0;
+    const int e1 = row[i + 1];
+#pragma unroll 4
+    for (int a = row[i]; a < e1; a++) {
+        const uint32_t e = adj[a];   // plain load: adj may be staged in shared memory
+        f += (int)(int8_t)(e & 0xffu) * sp[e >> 8];
+    }
+    return f;
+}
+
 // --------------------------------------------------------------- sweeps
 // Colour-class Metropolis sweep of the block's replicas (production).
 // dE_i = -2 s_i (h_i + f_i); accepted with probability min(1, exp(-beta dE))
@@ -550,11 +564,11 @@ __device__ void colored_sweep(const EngineArgs& A, const BlockCtx& B, unsigned l
         const int Sc = s_col[c + 1] - c0;
         if (ONE) {
             int8_t* sp = B.spin;
-            int32_t* fd = B.field;
+            int32_t* fd = B.field;   // null in field_gather mode
             const uint32_t* thr_row = s_thr + B.tb[0];
             for (int i = c0 + tid; i < c0 + Sc; i += T) {
                 const int s = sp[i];
-                const int f = fd[i] + (D.has_h ? B.h[i] : 0);
+                const int f = (fd ? fd[i] : gather_field(row, adj, sp, i)) + (D.has_h ? B.h[i] : 0);
                 const int de = -2 * s * f;
                 bool acc = de <= 0;
                 if (!acc) {
@@ -565,12 +579,14 @@ __device__ void colored_sweep(const EngineArgs& A, const BlockCtx& B, unsigned l
                     sp[i] = (int8_t)-s;
                     acc_de += de;
                     acc_fl++;
-                    const int dl = -2 * s;
-                    const int e1 = row[i + 1];
+                    if (fd) {
+                        const int dl = -2 * s;
+                        const int e1 = row[i + 1];
 #pragma unroll 4
-                    for (int a = row[i]; a < e1; a++) {
-                        const uint32_t e = adj[a];
-                        atomicAdd(fd + (e >> 8), (int)(int8_t)(e & 0xffu) * dl);
+                        for (int a = row[i]; a < e1; a++) {
+                            const uint32_t e = adj[a];
+                            atomicAdd(fd + (e >> 8), (int)(int8_t)(e & 0xffu) * dl);
+                        }
                     }
                 }
             }
@@ -584,9 +600,9 @@ __device__ void colored_sweep(const EngineArgs& A, const BlockCtx& B, unsigned l
                     j = it / Sc;
                     const int i = c0 + (it - j * Sc);
                     int8_t* sp = B.spin + j * npad;
-                    int32_t* fd = B.field + j * npad;
+                    int32_t* fd = B.field ? B.field + j * npad : nullptr;
                     const int s = sp[i];
-                    const int f = fd[i] + (D.has_h ? B.h[i] : 0);
+                    const int f = (fd ? fd[i] : gather_field(row, adj, sp, i)) + (D.has_h ? B.h[i] : 0);
                     de = -2 * s * f;
                     acc = de <= 0;
                     if (!acc) {
@@ -595,11 +611,13 @@ __device__ void colored_sweep(const EngineArgs& A, const BlockCtx& B, unsigned l
                     }
                     if (acc) {
                         sp[i] = (int8_t)-s;
-                        const int dl = -2 * s;
-                        const int e1 = row[i + 1];
-                        for (int a = row[i]; a < e1; a++) {
-                            const uint32_t e = adj[a];
-                            atomicAdd(fd + (e >> 8), (int)(int8_t)(e & 0xffu) * dl);
+                        if (fd) {
+                            const int dl = -2 * s;
+                            const int e1 = row[i + 1];
+                            for (int a = row[i]; a < e1; a++) {
+                                const uint32_t e = adj[a];
+                                atomicAdd(fd + (e >> 8), (int)(int8_t)(e & 0xffu) * dl);
+                            }
                         }
                     }
                 }
@@ -936,9 +954,11 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
         B.field = A.fields + D.spin_off + (long long)B.r0 * D.n_pad;
     } else {
         B.spin = sm_ptr<int8_t>(smem, S.spin);
-        B.field = sm_ptr<int32_t>(smem, S.field);
+        B.field = S.field_gather ? nullptr : sm_ptr<int32_t>(smem, S.field);
     }
-    uint32_t* s_thr = sm_ptr<uint32_t>(smem, S.thr);
+    // acceptance thresholds: shared memory, or read through L1 (field_gather)
+    uint32_t* s_thr_w = sm_ptr<uint32_t>(smem, S.thr);
+    const uint32_t* s_thr = S.field_gather ? A.thr + D.thr_off : s_thr_w;
     double* s_ptab = sm_ptr<double>(smem, S.ptab);
     B.slot = sm_ptr<uint32_t>(smem, S.slot);
     B.rslot = sm_ptr<uint32_t>(smem, S.rslot);
@@ -958,7 +978,8 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
     uint32_t* s_xrand = sm_ptr<uint32_t>(smem, S.xrand);
     int* s_lvl = sm_ptr<int>(smem, S.xlevel);
     uint32_t* s_tmp = sm_ptr<uint32_t>(smem, S.xpos);
-    uint8_t* s_icm = S.state_global ? A.icm_pool + (size_t)blockIdx.x * (size_t)A.icm_pool_stride : smem + S.icm;
+    uint8_t* s_icm = (S.state_global || S.field_gather) ? A.icm_pool + (size_t)blockIdx.x * (size_t)A.icm_pool_stride
+                                                          : smem + S.icm;
     int* s_misc = sm_ptr<int>(smem, S.misc);
     long long* s_mag = sm_ptr<long long>(smem, S.mag);
     long long* s_team_acc = sm_ptr<long long>(smem, S.misc + 64);
@@ -1002,7 +1023,7 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
         const long long base = D.spin_off + (long long)B.r0 * npad;
         for (int idx = tid; idx < rpc * npad; idx += T) {
             B.spin[idx] = A.spins[base + idx];
-            B.field[idx] = A.fields[base + idx];
+            if (B.field) B.field[idx] = A.fields[base + idx];
         }
     }
     for (int r = tid; r < R; r += T) {
@@ -1016,7 +1037,7 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
         s_beta[k] = A.beta[D.beta_off + k];
     }
     for (int k = tid; k < nt * kst; k += T) {
-        s_thr[k] = A.thr[D.thr_off + k];
+        if (!S.field_gather) s_thr_w[k] = A.thr[D.thr_off + k];
         if (REPLAY) s_ptab[k] = A.ptab[D.ptab_off + k];
     }
     for (int j = tid; j < rpc; j += T) {
@@ -1184,7 +1205,14 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
         const long long base = D.spin_off + (long long)B.r0 * npad;
         for (int idx = tid; idx < rpc * npad; idx += T) {
             A.spins[base + idx] = B.spin[idx];
-            A.fields[base + idx] = B.field[idx];
+            if (B.field) A.fields[base + idx] = B.field[idx];
+        }
+        if (S.field_gather) {
+            // the stored fields of the master copy, gathered once per launch
+            for (int idx = tid; idx < rpc * npad; idx += T) {
+                const int j = idx / npad, i = idx - j * npad;
+                A.fields[base + idx] = i < n ? gather_field(B.row, B.adj, B.spin + (long long)j * npad, i) : 0;
+            }
         }
     }
     for (int j = tid; j < rpc; j += T) {

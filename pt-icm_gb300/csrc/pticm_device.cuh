@@ -127,11 +127,13 @@ struct ThreadRng12 {
     uint4 ctr;   // (thread id, sweep lo, sweep hi, call index)
     uint2 key;
 
+    // The first block of uniforms is generated at the first draw: a thread
+    // whose moves are all downhill never runs Philox (the stream is the same).
     __device__ __forceinline__ void start(uint2 k, uint32_t tid, unsigned long long sweep, uint32_t call0 = 0u) {
         key = k;
         ctr = make_uint4(tid, (uint32_t)sweep, (uint32_t)(sweep >> 32), 0u);
         calls = call0;
-        refill();
+        avail = 0;
     }
     __device__ __forceinline__ void refill() {
         uint4 a = ctr, b = ctr, c = ctr;

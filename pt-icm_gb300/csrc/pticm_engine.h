@@ -70,6 +70,8 @@ struct SmemPlan {
     uint32_t misc;
     int32_t stage_adj;
     int32_t state_global;       // replica spins/fields and ICM scratch in device memory (large instances)
+    int32_t field_gather;       // spins in shared memory, no stored fields: each visit gathers the local
+                                // field from the neighbours' spins; ICM scratch and thresholds in device memory
     int32_t teams;              // ICM teams (warps, or one block-wide team)
     int32_t max_n_pad, max_kmax, max_R, max_nt;
 };

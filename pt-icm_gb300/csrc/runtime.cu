@@ -157,9 +157,10 @@ SmemPlan layout_plan(const PlanDims& d) {
     S.col = take((d.ncolors + 1) * 4);
     S.h = take(d.n_h * 4);
     S.state_global = d.state_global ? 1 : 0;
+    S.field_gather = d.field_gather ? 1 : 0;
     S.spin = take(d.state_global ? 0 : d.spin_sites);
-    S.field = take(d.state_global ? 0 : d.spin_sites * 4);
-    S.thr = take(d.nt_kst * 4);
+    S.field = take((d.state_global || d.field_gather) ? 0 : d.spin_sites * 4);
+    S.thr = take(d.field_gather ? 0 : d.nt_kst * 4);
     S.ptab = take(d.replay ? d.nt_kst * 8 : 0);
     S.slot = take(d.R * 4);
     S.rslot = take(d.rpc * 8);
@@ -180,7 +181,7 @@ SmemPlan layout_plan(const PlanDims& d) {
     S.xpos = take(d.nt * 4);
     S.icm_team_bytes = icm_team_bytes((int32_t)d.max_n_pad);
     S.teams = d.teams;
-    S.icm = take(d.state_global ? 0 : d.icm_bytes);
+    S.icm = take((d.state_global || d.field_gather) ? 0 : d.icm_bytes);
     S.mag = take(d.rpc * 8);
     S.misc = take(64 + 8 * 32 + 4 * 64 + 64);
     S.total = (uint32_t)off;
@@ -191,10 +192,12 @@ SmemPlan layout_plan(const PlanDims& d) {
     return S;
 }
 
-SmemPlan make_plan(const InstanceDesc& D, bool replay, int teams, int threads, bool stage_adj, bool state_global) {
+SmemPlan make_plan(const InstanceDesc& D, bool replay, int teams, int threads, bool stage_adj, bool state_global,
+                   bool field_gather) {
     PlanDims d;
     d.replay = replay;
     d.state_global = state_global;
+    d.field_gather = field_gather;
     d.add(D, stage_adj, teams);
     (void)threads;
     return layout_plan(d);
@@ -255,6 +258,32 @@ int choose_config(const HostProblem& P, const pticm_opts& o, bool replay, Instan
         if (replay) {
             msg = "replay needs the replicas in shared memory; the instance is too large";
             return PTICM_ERR_UNSUPPORTED;
+        }
+        // first choice: the spins alone in shared memory, fields gathered
+        // at each visit (no field atomics), one replica per block
+        if (o.replicas_per_block == 0 && o.block_threads == 0) {
+            bool gathered = false;
+            for (int t : {1024, 512, 256, 128}) {
+                InstanceDesc d1 = D;
+                d1.rpc = 1;
+                d1.group = R;
+                const SmemPlan p1 = make_plan(d1, false, 1, t, false, false, true);
+                if (p1.total > kSmemLimit) continue;
+                int per_sm = 0;
+                if (engine_max_blocks_per_sm(false, true, t, p1.total, &per_sm) != cudaSuccess) continue;
+                if ((int64_t)per_sm * sms < R) continue;
+                rpc = 1;
+                threads = t;
+                block_team = true;
+                teams = 1;
+                plan = p1;
+                gathered = true;
+                break;
+            }
+            if (gathered) {
+                cfg.field_gather = true;
+                break;
+            }
         }
         global = true;
         // with the state in device memory a block needs little shared
@@ -398,7 +427,7 @@ int configure(pticm_ctx* c, bool replay) {
     c->block_team = cfg.block_team;
     c->plan = cfg.plan;
     finish_desc(c->desc, c->P, c->o, cfg);
-    if (cfg.state_global) {
+    if (cfg.state_global || cfg.field_gather) {
         c->icm_stride = (long long)cfg.teams * icm_team_bytes(c->desc.n_pad);
         const size_t want = (size_t)cfg.group * (size_t)c->icm_stride;
         if (c->d_icm_pool.n != want) CK(c->d_icm_pool.alloc(want));

@@ -167,13 +167,15 @@ __device__ __forceinline__ IcmScratch icm_scratch(uint8_t* base, int n_pad) {
 // reference's global-flip rule (src/icm.cc:20-28: more than n/2 differing
 // sites -> negate A), a seed uniform among differing sites (src/icm.cc:33;
 // here the differing site with the smallest per-site random key, which is
-// uniform), then grows the seed's cluster of differing sites breadth-first
-// (src/icm.cc:37-72 grows it depth-first; the cluster is the same set),
-// flipping each member in both replicas as it is reached.  Fields are
-// updated per flip; energies change by -2 s_u h_u per flipped site plus
-// -2 J s_u s_v per edge to a non-cluster neighbour (equal in A and B), an
-// exact integer update.  Members held by another block are read from the
-// published copy and flipped by their own block, which grows the same set.
+// uniform), then finds the seed's cluster C of differing sites -- breadth-
+// first, or by labelling the components of the whole overlap (src/icm.cc:
+// 37-72 grows it depth-first; the cluster is the same set) -- and flips the
+// smaller of C and the rest of the overlap in both replicas.  Fields are
+// updated per flipped site (or recomputed when the set is large); energies
+// change by -2 s_u h_u per flipped site plus -2 J s_u s_v per edge leaving
+// the set (s_v equal in A and B), an exact integer update.  Members held by
+// another block are read from the published copy and flipped by their own
+// block, which finds the same set.
 template <bool BLOCK, bool REPLAY>
 __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK>& team, int q,
                          int rA, int rB, unsigned long long step, int ls, const IcmScratch& X,
@@ -203,9 +205,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
     }
     long long cnt = 0, hs = 0;
     unsigned long long kd = ~0ull, ke = ~0ull;
-    for (int i = team.tr; i < n; i += team.ts) {
-        const int8_t a = locA ? sA[i] : ld_cg(pubA + i);
-        const int8_t b = locB ? sB[i] : ld_cg(pubB + i);
+    auto overlap_site = [&](int i, int8_t a, int8_t b) {
         const bool di = a != b;
         d[i] = di;
         cnt += di;
@@ -216,6 +216,20 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
             else ke = min(ke, key);
         }
         if (D.has_h && locA) hs += (long long)B.h[i] * a;
+    };
+    // two sites per round, both loaded first: the partner's spins come from
+    // the published copy in L2
+    for (int i = team.tr; i < n; i += 2 * team.ts) {
+        const int i2 = i + team.ts;
+        const int8_t a = locA ? sA[i] : ld_cg(pubA + i);
+        const int8_t b = locB ? sB[i] : ld_cg(pubB + i);
+        int8_t a2 = 0, b2 = 0;
+        if (i2 < n) {
+            a2 = locA ? sA[i2] : ld_cg(pubA + i2);
+            b2 = locB ? sB[i2] : ld_cg(pubB + i2);
+        }
+        overlap_site(i, a, b);
+        if (i2 < n) overlap_site(i2, a2, b2);
     }
     for (int w = team.tr; w < nwords; w += team.ts) X.vis[w] = 0u;
     team.reduce(cnt, kd, ke, hs);
@@ -261,125 +275,192 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
     const int algo = D.icm_algo;
     bool absolute = false;   // energies set from scratch (large flipped sets)
     int swapped = 0;         // the flipped set was D\C (the chains hold each other's result)
-    if (cnt > 0 && algo != ENGINE_ICM_BFS) {
-        // label the components of the whole overlap subgraph, then flip the
-        // sites sharing the seed's label
-        int* lab = X.queue;
-        volatile int* vl = lab;
-        bool ok = true;
-        for (int i = team.tr; i < n; i += team.ts) lab[i] = d[i] ? i : n;
-        team.sync();
-        if (algo == ENGINE_ICM_UNION_FIND) {
-            // Afforest (Sutton, Ben-Nun, Barak, IPDPS 2018): link every
-            // overlap site to its first two overlap neighbours, compress,
-            // take the most frequent root of a sample as the large component
-            // L, then process the full adjacency only of sites outside L.  An
-            // edge skipped at an end in L is processed from its other end,
-            // unless that end is in L too -- then both are already joined.
-            for (int u = team.tr; u < n; u += team.ts) {
-                if (!d[u]) continue;
-                int k = 0;
-                const int e1 = B.row[u + 1];
-                for (int a = B.row[u]; a < e1 && k < 2; a++) {
-                    const int v = (int)(B.adj[a] >> 8);
-                    if (d[v]) {
-                        ok &= uf_unite(lab, u, v);
-                        k++;
-                    }
-                }
+    if (cnt > 0) {
+        long long csize = 0;
+        if (algo == ENGINE_ICM_BFS) {
+            // breadth-first search from the seed; members of C get d = 2
+            // (the visited bits make each site's claim unique)
+            volatile int* vctl = team.ctl;
+            if (team.tr == 0) {
+                X.queue[0] = seed;
+                X.vis[seed >> 5] |= 1u << (seed & 31);
+                d[seed] = 2;
+                vctl[1] = 1;
             }
             team.sync();
-            for (int u = team.tr; u < n; u += team.ts) {
-                if (!d[u]) continue;
-                const int r = uf_find(vl, u);
-                if (r < 0) ok = false;
-                else vl[u] = r;
-            }
-            team.sync();
-            if (team.tr < 32) {
-                // vote over 32 sampled overlap sites (one warp)
-                int cand = -1;
-                const int i0 = (int)(((long long)team.tr * n) >> 5);
-                for (int t = 0; t < 32 && i0 + t < n; t++)
-                    if (d[i0 + t]) { cand = vl[i0 + t]; break; }
-                const unsigned grp = __match_any_sync(0xffffffffu, cand);
-                int votes = cand >= 0 ? __popc(grp) : 0, best = cand;
-                for (int o = 16; o > 0; o >>= 1) {
-                    const int ov = __shfl_xor_sync(0xffffffffu, votes, o);
-                    const int oc = __shfl_xor_sync(0xffffffffu, best, o);
-                    if (ov > votes || (ov == votes && oc < best)) { votes = ov; best = oc; }
-                }
-                if (team.tr == 0) team.ctl[0] = best;
-            }
-            team.sync();
-            const int L = *(volatile int*)team.ctl;
-            for (int u = team.tr; u < n; u += team.ts) {
-                if (!d[u]) continue;
-                if (uf_find(vl, u) == L) continue;
-                const int e1 = B.row[u + 1];
-#pragma unroll 4
-                for (int a = B.row[u]; a < e1; a++) {
-                    const int v = (int)(B.adj[a] >> 8);
-                    if (d[v]) ok &= uf_unite(lab, u, v);
-                }
-            }
-            team.sync();
-        } else {
-            // minimum-label propagation with root hooking and pointer jumping
-            // (Shiloach-Vishkin style); labels only decrease and always name
-            // a site of the same component
-            bool conv = false;
-            for (int round = 0; round < 512 && !conv; round++) {
-                int changed = 0;
-                for (int u = team.tr; u < n; u += team.ts) {
-                    if (!d[u]) continue;
-                    const int lu = vl[u];
-                    int best = lu;
-                    const int e1 = B.row[u + 1];
-#pragma unroll 4
-                    for (int a = B.row[u]; a < e1; a++) {
-                        const int v = (int)(B.adj[a] >> 8);
-                        const int lv = vl[v];
-                        if (d[v]) best = min(best, lv);
+            const int lane = threadIdx.x & 31;
+            int lo = 0;
+            for (int level = 0; level <= n; level++) {
+                const int hi = vctl[1];
+                team.sync();
+                if (lo == hi) break;
+                for (int base = lo; base < hi; base += team.ts) {
+                    const int idx = base + team.tr;
+                    const bool have = idx < hi;
+                    const int u = have ? X.queue[idx] : 0;
+                    const int e0 = have ? B.row[u] : 0;
+                    const int deg = have ? B.row[u + 1] - e0 : 0;
+                    for (int k = 0; __any_sync(0xffffffffu, k < deg); k++) {
+                        bool found = false;
+                        int v = 0;
+                        if (k < deg) {
+                            v = (int)(B.adj[e0 + k] >> 8);
+                            if (((volatile uint8_t*)d)[v] == 1) {
+                                const uint32_t bit = 1u << (v & 31);
+                                found = !(atomicOr(X.vis + (v >> 5), bit) & bit);
+                            }
+                        }
+                        const unsigned m = __ballot_sync(0xffffffffu, found);
+                        if (m) {
+                            const int leader = __ffs(m) - 1;
+                            int slot0 = 0;
+                            if (lane == leader) slot0 = atomicAdd(team.ctl + 1, __popc(m));
+                            slot0 = __shfl_sync(0xffffffffu, slot0, leader);
+                            if (found) {
+                                X.queue[slot0 + __popc(m & ((1u << lane) - 1u))] = v;
+                                d[v] = 2;
+                            }
+                        }
                     }
-                    if (best < lu) {
-                        atomicMin(lab + lu, best);
-                        atomicMin(lab + u, best);
-                        changed = 1;
-                    }
-                }
-                conv = !(BLOCK ? (__syncthreads_or(changed) != 0) : (__any_sync(0xffffffffu, changed) != 0));
-                if (!BLOCK) __syncwarp();
-                for (int u = team.tr; u < n; u += team.ts) {
-                    if (!d[u]) continue;
-                    int l = vl[u];
-                    for (int g = 0; g < n; g++) {
-                        const int ll = vl[l];
-                        if (ll >= l) break;
-                        l = ll;
-                    }
-                    vl[u] = l;
                 }
                 team.sync();
+                lo = hi;
             }
-            ok = conv;
-        }
-        if (!ok) dev_fail(A.status, A.abort_flag, DEV_UF_LIMIT, where_err + 3, q, algo);
-        if (threadIdx.x == 0) P.subtick(PROF_ICM_UNION);
-        const int root = (algo == ENGINE_ICM_UNION_FIND) ? uf_find(vl, seed) : vl[seed];
-        // mark the cluster C (d = 2) and count it
-        long long csize = 0;
-        for (int u = team.tr; u < n; u += team.ts) {
-            if (!d[u]) continue;
-            const int lu = (algo == ENGINE_ICM_UNION_FIND) ? uf_find(vl, u) : vl[u];
-            if (lu != root) continue;
-            d[u] = 2;
-            csize++;
-        }
-        {
-            unsigned long long m1 = ~0ull, m2 = ~0ull;
-            long long none = 0;
-            team.reduce(csize, m1, m2, none);
+            csize = lo;
+            if (threadIdx.x == 0) P.subtick(PROF_ICM_UNION);
+        } else {
+            // label the components of the whole overlap subgraph, then mark the
+            // sites sharing the seed's label
+            int* lab = X.queue;
+            volatile int* vl = lab;
+            bool ok = true;
+            for (int i = team.tr; i < n; i += team.ts) lab[i] = d[i] ? i : n;
+            team.sync();
+            if (algo == ENGINE_ICM_UNION_FIND) {
+                // Afforest (Sutton, Ben-Nun, Barak, IPDPS 2018): in two
+                // rounds, link every overlap site to its r-th overlap
+                // neighbour and compress the trees; take the most frequent
+                // root of a sample as the large component L, then process the
+                // full adjacency only of sites outside L.  An edge skipped at
+                // an end in L is processed from its other end, unless that end
+                // is in L too -- then both are already joined.
+                for (int round = 0; round < 2; round++) {
+                    for (int u = team.tr; u < n; u += team.ts) {
+                        if (!d[u]) continue;
+                        int k = 0;
+                        const int e1 = B.row[u + 1];
+                        for (int a = B.row[u]; a < e1; a++) {
+                            const int v = (int)(B.adj[a] >> 8);
+                            if (!d[v]) continue;
+                            if (k++ == round) {
+                                ok &= uf_unite(lab, u, v);
+                                break;
+                            }
+                        }
+                    }
+                    team.sync();
+                    for (int u = team.tr; u < n; u += team.ts) {
+                        if (!d[u]) continue;
+                        const int r = uf_find(vl, u);
+                        if (r < 0) ok = false;
+                        else vl[u] = r;
+                    }
+                    team.sync();
+                }
+                if (team.tr < 32) {
+                    // vote over 32 sampled overlap sites (one warp)
+                    // each lane samples the first overlap site in a 32-byte
+                    // window of the flags (eight independent word loads; the
+                    // flags start on 16 bytes, bytes from n on are masked)
+                    int cand = -1;
+                    const int w0 = (int)(((long long)team.tr * n) >> 7);
+                    uint32_t fw[8];
+#pragma unroll
+                    for (int j = 0; j < 8; j++)
+                        fw[j] = 4 * (w0 + j) < n ? reinterpret_cast<const uint32_t*>(d)[w0 + j] : 0u;
+                    for (int j = 0; j < 8 && cand < 0; j++)
+                        for (int b = 0; b < 4; b++) {
+                            const int i = 4 * (w0 + j) + b;
+                            if (i < n && ((fw[j] >> (8 * b)) & 0xffu)) { cand = vl[i]; break; }
+                        }
+                    const unsigned grp = __match_any_sync(0xffffffffu, cand);
+                    int votes = cand >= 0 ? __popc(grp) : 0, best = cand;
+                    for (int o = 16; o > 0; o >>= 1) {
+                        const int ov = __shfl_xor_sync(0xffffffffu, votes, o);
+                        const int oc = __shfl_xor_sync(0xffffffffu, best, o);
+                        if (ov > votes || (ov == votes && oc < best)) { votes = ov; best = oc; }
+                    }
+                    if (team.tr == 0) team.ctl[0] = best;
+                }
+                team.sync();
+                const int L = *(volatile int*)team.ctl;
+                for (int u = team.tr; u < n; u += team.ts) {
+                    if (!d[u]) continue;
+                    if (uf_find(vl, u) == L) continue;
+                    const int e1 = B.row[u + 1];
+    #pragma unroll 4
+                    for (int a = B.row[u]; a < e1; a++) {
+                        const int v = (int)(B.adj[a] >> 8);
+                        if (d[v]) ok &= uf_unite(lab, u, v);
+                    }
+                }
+                team.sync();
+            } else {
+                // minimum-label propagation with root hooking and pointer jumping
+                // (Shiloach-Vishkin style); labels only decrease and always name
+                // a site of the same component
+                bool conv = false;
+                for (int round = 0; round < 512 && !conv; round++) {
+                    int changed = 0;
+                    for (int u = team.tr; u < n; u += team.ts) {
+                        if (!d[u]) continue;
+                        const int lu = vl[u];
+                        int best = lu;
+                        const int e1 = B.row[u + 1];
+    #pragma unroll 4
+                        for (int a = B.row[u]; a < e1; a++) {
+                            const int v = (int)(B.adj[a] >> 8);
+                            const int lv = vl[v];
+                            if (d[v]) best = min(best, lv);
+                        }
+                        if (best < lu) {
+                            atomicMin(lab + lu, best);
+                            atomicMin(lab + u, best);
+                            changed = 1;
+                        }
+                    }
+                    conv = !(BLOCK ? (__syncthreads_or(changed) != 0) : (__any_sync(0xffffffffu, changed) != 0));
+                    if (!BLOCK) __syncwarp();
+                    for (int u = team.tr; u < n; u += team.ts) {
+                        if (!d[u]) continue;
+                        int l = vl[u];
+                        for (int g = 0; g < n; g++) {
+                            const int ll = vl[l];
+                            if (ll >= l) break;
+                            l = ll;
+                        }
+                        vl[u] = l;
+                    }
+                    team.sync();
+                }
+                ok = conv;
+            }
+            if (!ok) dev_fail(A.status, A.abort_flag, DEV_UF_LIMIT, where_err + 3, q, algo);
+            if (threadIdx.x == 0) P.subtick(PROF_ICM_UNION);
+            const int root = (algo == ENGINE_ICM_UNION_FIND) ? uf_find(vl, seed) : vl[seed];
+            // mark the cluster C (d = 2) and count it
+            for (int u = team.tr; u < n; u += team.ts) {
+                if (!d[u]) continue;
+                const int lu = (algo == ENGINE_ICM_UNION_FIND) ? uf_find(vl, u) : vl[u];
+                if (lu != root) continue;
+                d[u] = 2;
+                csize++;
+            }
+            {
+                unsigned long long m1 = ~0ull, m2 = ~0ull;
+                long long none = 0;
+                team.reduce(csize, m1, m2, none);
+            }
         }
         // (A, B) -> (A flipped on C, B flipped on C) is the same pair of
         // states as (B flipped on D\C, A flipped on D\C): flip the smaller of
@@ -446,68 +527,6 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
             }
         }
         team.sync();
-    }
-    if (cnt > 0 && algo == ENGINE_ICM_BFS) {
-        // breadth-first growth of the seed's cluster, flipping as it goes
-        if (team.tr == 0) {
-            X.queue[0] = seed;
-            X.vis[seed >> 5] |= 1u << (seed & 31);
-            team.ctl[0] = 0;
-            team.ctl[1] = 1;
-        }
-        team.sync();
-        volatile int* vctl = team.ctl;
-        const int lane = threadIdx.x & 31;
-        for (int level = 0; level <= n; level++) {
-            const int lo = vctl[0], hi = vctl[1];
-            team.sync();
-            if (lo == hi) break;
-            for (int base = lo; base < hi; base += team.ts) {
-                const int idx = base + team.tr;
-                const bool have = idx < hi;
-                const int u = have ? X.queue[idx] : 0;
-                int sa = 0, sb = 0, e0 = 0, deg = 0;
-                if (have) {
-                    const int hu = D.has_h ? B.h[u] : 0;
-                    if (locA) { sa = sA[u]; sA[u] = (int8_t)-sa; dEa -= 2 * sa * hu; }
-                    if (locB) { sb = sB[u]; sB[u] = (int8_t)-sb; dEb -= 2 * sb * hu; }
-                    e0 = B.row[u];
-                    deg = B.row[u + 1] - e0;
-                }
-                for (int k = 0; __any_sync(0xffffffffu, k < deg); k++) {
-                    bool found = false;
-                    int v = 0;
-                    if (k < deg) {
-                        const uint32_t e = B.adj[e0 + k];
-                        v = (int)(e >> 8);
-                        const int J = (int)(int8_t)(e & 0xffu);
-                        if (fA) atomicAdd(fA + v, J * (-2 * sa));
-                        if (fB) atomicAdd(fB + v, J * (-2 * sb));
-                        if (d[v]) {
-                            const uint32_t bit = 1u << (v & 31);
-                            found = !(atomicOr(X.vis + (v >> 5), bit) & bit);
-                        } else {
-                            // edge leaving the cluster: s_v is equal in A and B
-                            const int sv = locA ? sA[v] : sB[v];
-                            if (locA) dEa -= 2 * J * sa * sv;
-                            if (locB) dEb -= 2 * J * sb * sv;
-                        }
-                    }
-                    const unsigned m = __ballot_sync(0xffffffffu, found);
-                    if (m) {
-                        const int leader = __ffs(m) - 1;
-                        int slot0 = 0;
-                        if (lane == leader) slot0 = atomicAdd(team.ctl + 1, __popc(m));
-                        slot0 = __shfl_sync(0xffffffffu, slot0, leader);
-                        if (found) X.queue[slot0 + __popc(m & ((1u << lane) - 1u))] = v;
-                    }
-                }
-            }
-            team.sync();
-            if (team.tr == 0) vctl[0] = hi;
-            team.sync();
-        }
-        if (threadIdx.x == 0) P.subtick(PROF_ICM_UNION);
     }
     if (!absolute && (gflip || cnt > 0)) {
         team.sum2(dEa, dEb);

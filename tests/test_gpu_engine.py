@@ -84,12 +84,13 @@ def test_evaluate_matches_oracle(pticm, g):
     assert bool(info.sparse) == orc.sparse
 
 
+@pytest.mark.parametrize("algo", [0, 1, 3])   # auto (union-find), breadth-first, label propagation
 @pytest.mark.parametrize("rpb", [0, 1])
 @pytest.mark.parametrize("g,T0,T1,nt", [("pmL20_c1.gset", 0.5, 3.0, 32), ("rnd200_w1", 0.5, 15.0, 12),
                                          ("lin40.ising", 0.5, 3.0, 8), ("pmL6.gset", 0.5, 3.0, 6)])
-def test_fields_exact_after_every_phase(pticm, g, T0, T1, nt, rpb):
+def test_fields_exact_after_every_phase(pticm, g, T0, T1, nt, rpb, algo):
     prob = pticm.Problem.load(os.path.join(GRAPHS, g))
-    ctx = pticm.Context(prob, nt=nt, seed=7, icm=True, replicas_per_block=rpb)
+    ctx = pticm.Context(prob, nt=nt, seed=7, icm=True, replicas_per_block=rpb, icm_algo=algo)
     ctx.set_ladder(pticm.beta_linspace(T0, T1, nt))
     ctx.init_states(11)
     assert ctx.verify() == 0
@@ -121,8 +122,9 @@ def _golden_runs():
         return [r for r in json.load(f) if not r["args"].get("preprocess")]
 
 
+@pytest.mark.parametrize("algo", [0, 1])   # the cluster is one set whichever search finds it
 @pytest.mark.parametrize("k", range(len(_golden_runs())))
-def test_replay_matches_reference_trajectory(pticm, k):
+def test_replay_matches_reference_trajectory(pticm, k, algo):
     run = _golden_runs()[k]
     kw = dict(run["args"])
     path = os.path.join(GRAPHS, run["graph"])
@@ -130,7 +132,8 @@ def test_replay_matches_reference_trajectory(pticm, k):
     tr = orc["trace"]
     nt = orc["Nt"]
     prob = pticm.Problem.load(path)
-    ctx = pticm.Context(prob, nt=nt, seed=kw["seed"], sweeps=kw.get("sweeps", 1), icm=kw.get("icm", False))
+    ctx = pticm.Context(prob, nt=nt, seed=kw["seed"], sweeps=kw.get("sweeps", 1), icm=kw.get("icm", False),
+                        icm_algo=algo)
     ctx.set_ladder(orc["beta"][:nt])
     ctx.set_states(tr["init_states"])
     ctx.replay(tr, kw["pts"])

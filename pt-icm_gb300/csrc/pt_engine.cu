@@ -84,11 +84,24 @@ __device__ __forceinline__ bool uf_unite(int* parent, int a, int b) {
 // ---------------------------------------------------------- team helpers
 // An ICM "team" is either one warp (many pairs per block) or the whole block
 // (one pair per block).  Block-wide reductions go through shared scratch.
+// A block team reduces through three slots of four words, used in turn: a
+// slot is reset by the reduction after the one that used it (whose barrier
+// every reader of the slot has passed), so one barrier per reduction
+// suffices.  Between teams all slots hold the identity (0, ~0, ~0, 0).
+__device__ __forceinline__ void team_slot_reset(long long* acc, int slot) {
+    unsigned long long* u = reinterpret_cast<unsigned long long*>(acc) + 4 * slot;
+    u[0] = 0;
+    u[1] = ~0ull;
+    u[2] = ~0ull;
+    u[3] = 0;
+}
+
 template <bool BLOCK>
 struct Team {
     int tr, ts;                  // rank and size
-    long long* acc;              // team scratch (shared, 4 words for a block team)
-    int* ctl;                    // team scratch (shared): BFS queue head and tail
+    long long* acc;              // team scratch (shared, 12 words for a block team)
+    int* ctl;                    // team scratch (shared): BFS queue tail, vote
+    mutable int k = 0;           // reductions so far (the same in every thread)
     __device__ __forceinline__ void sync() const {
         if (BLOCK) __syncthreads(); else __syncwarp();
     }
@@ -102,10 +115,8 @@ struct Team {
             s3 += __shfl_xor_sync(0xffffffffu, s3, o);
         }
         if (!BLOCK) return;
-        unsigned long long* u = reinterpret_cast<unsigned long long*>(acc);
-        __syncthreads();
-        if (threadIdx.x == 0) { u[0] = 0; u[1] = ~0ull; u[2] = ~0ull; u[3] = 0; }
-        __syncthreads();
+        const int slot = k % 3;
+        unsigned long long* u = reinterpret_cast<unsigned long long*>(acc) + 4 * slot;
         if ((threadIdx.x & 31) == 0) {
             atomicAdd(u + 0, (unsigned long long)s0);
             atomicMin(u + 1, m1);
@@ -114,7 +125,8 @@ struct Team {
         }
         __syncthreads();
         s0 = (long long)u[0]; m1 = u[1]; m2 = u[2]; s3 = (long long)u[3];
-        __syncthreads();
+        if (threadIdx.x == 0 && k > 0) team_slot_reset(acc, (k + 2) % 3);
+        k++;
     }
     __device__ __forceinline__ void sum2(long long& a, long long& b) const {
         unsigned long long x = ~0ull, y = ~0ull;
@@ -151,6 +163,7 @@ struct IcmScratch {
     int* queue;
     uint8_t* d;
     uint32_t* vis;
+    int* list;          // block team only: overlap sites first, the others from the end
 };
 
 __device__ __forceinline__ IcmScratch icm_scratch(uint8_t* base, int n_pad) {
@@ -158,6 +171,7 @@ __device__ __forceinline__ IcmScratch icm_scratch(uint8_t* base, int n_pad) {
     X.queue = reinterpret_cast<int*>(base);
     X.d = base + (size_t)n_pad * 4;
     X.vis = reinterpret_cast<uint32_t*>(base + (size_t)n_pad * 5);
+    X.list = reinterpret_cast<int*>(base + icm_team_bytes(n_pad));
     return X;
 }
 
@@ -217,23 +231,59 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
         }
         if (D.has_h && locA) hs += (long long)B.h[i] * a;
     };
+    // a block team lists the overlap sites (from the front) and the others
+    // (from the back), so that its later passes visit overlap sites only;
+    // the counters are team.ctl[2..3], zero between pairs
+    int* lst = X.list;
+    auto append = [&](bool valid, bool di, int i) {
+        const int lane = threadIdx.x & 31;
+        const unsigned mf = __ballot_sync(0xffffffffu, valid && di);
+        const unsigned mb = __ballot_sync(0xffffffffu, valid && !di);
+        int f0 = 0, b0 = 0;
+        if (lane == 0) {
+            if (mf) f0 = atomicAdd(team.ctl + 2, __popc(mf));
+            if (mb) b0 = atomicAdd(team.ctl + 3, __popc(mb));
+        }
+        f0 = __shfl_sync(0xffffffffu, f0, 0);
+        b0 = __shfl_sync(0xffffffffu, b0, 0);
+        const unsigned lt = (1u << lane) - 1u;
+        const int pf = f0 + __popc(mf & lt), pb = n - 1 - b0 - __popc(mb & lt);
+        if (valid && di && pf < n) lst[pf] = i;
+        if (valid && !di && pb >= 0) lst[pb] = i;
+    };
     // two sites per round, both loaded first: the partner's spins come from
     // the published copy in L2
-    for (int i = team.tr; i < n; i += 2 * team.ts) {
-        const int i2 = i + team.ts;
-        const int8_t a = locA ? sA[i] : ld_cg(pubA + i);
-        const int8_t b = locB ? sB[i] : ld_cg(pubB + i);
-        int8_t a2 = 0, b2 = 0;
+    for (int base = 0; base < n; base += 2 * team.ts) {
+        const int i = base + team.tr, i2 = i + team.ts;
+        int8_t a = 0, b = 0, a2 = 0, b2 = 0;
+        if (i < n) {
+            a = locA ? sA[i] : ld_cg(pubA + i);
+            b = locB ? sB[i] : ld_cg(pubB + i);
+        }
         if (i2 < n) {
             a2 = locA ? sA[i2] : ld_cg(pubA + i2);
             b2 = locB ? sB[i2] : ld_cg(pubB + i2);
         }
-        overlap_site(i, a, b);
+        if (i < n) overlap_site(i, a, b);
         if (i2 < n) overlap_site(i2, a2, b2);
+        if (BLOCK) {
+            append(i < n, a != b, i);
+            append(i2 < n, a2 != b2, i2);
+        }
     }
     for (int w = team.tr; w < nwords; w += team.ts) X.vis[w] = 0u;
     team.reduce(cnt, kd, ke, hs);
     const bool gflip = cnt > (long long)(n / 2);
+    // the overlap list of a block team: [l0, l0 + llen) of lst
+    const int l0 = gflip ? (int)cnt : 0, llen = gflip ? n - (int)cnt : (int)cnt;
+    auto for_overlap = [&](auto&& f) {
+        if (BLOCK) {
+            for (int t = team.tr; t < llen; t += team.ts) f(lst[l0 + t]);
+        } else {
+            for (int u = team.tr; u < n; u += team.ts)
+                if (d[u]) f(u);
+        }
+    };
     long long dEa = 0, dEb = 0;
     if (gflip) {
         for (int i = team.tr; i < n; i += team.ts) {
@@ -334,7 +384,9 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
             int* lab = X.queue;
             volatile int* vl = lab;
             bool ok = true;
-            for (int i = team.tr; i < n; i += team.ts) lab[i] = d[i] ? i : n;
+            if (algo == ENGINE_ICM_UNION_FIND) for_overlap([&](int u) { lab[u] = u; });
+            else
+                for (int i = team.tr; i < n; i += team.ts) lab[i] = d[i] ? i : n;
             team.sync();
             if (algo == ENGINE_ICM_UNION_FIND) {
                 // Afforest (Sutton, Ben-Nun, Barak, IPDPS 2018): in two
@@ -345,8 +397,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                 // an end in L is processed from its other end, unless that end
                 // is in L too -- then both are already joined.
                 for (int round = 0; round < 2; round++) {
-                    for (int u = team.tr; u < n; u += team.ts) {
-                        if (!d[u]) continue;
+                    for_overlap([&](int u) {
                         int k = 0;
                         const int e1 = B.row[u + 1];
                         for (int a = B.row[u]; a < e1; a++) {
@@ -357,14 +408,13 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                                 break;
                             }
                         }
-                    }
+                    });
                     team.sync();
-                    for (int u = team.tr; u < n; u += team.ts) {
-                        if (!d[u]) continue;
+                    for_overlap([&](int u) {
                         const int r = uf_find(vl, u);
                         if (r < 0) ok = false;
                         else vl[u] = r;
-                    }
+                    });
                     team.sync();
                 }
                 if (team.tr < 32) {
@@ -394,16 +444,15 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                 }
                 team.sync();
                 const int L = *(volatile int*)team.ctl;
-                for (int u = team.tr; u < n; u += team.ts) {
-                    if (!d[u]) continue;
-                    if (uf_find(vl, u) == L) continue;
+                for_overlap([&](int u) {
+                    if (uf_find(vl, u) == L) return;
                     const int e1 = B.row[u + 1];
-    #pragma unroll 4
+#pragma unroll 4
                     for (int a = B.row[u]; a < e1; a++) {
                         const int v = (int)(B.adj[a] >> 8);
                         if (d[v]) ok &= uf_unite(lab, u, v);
                     }
-                }
+                });
                 team.sync();
             } else {
                 // minimum-label propagation with root hooking and pointer jumping
@@ -417,7 +466,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                         const int lu = vl[u];
                         int best = lu;
                         const int e1 = B.row[u + 1];
-    #pragma unroll 4
+#pragma unroll 4
                         for (int a = B.row[u]; a < e1; a++) {
                             const int v = (int)(B.adj[a] >> 8);
                             const int lv = vl[v];
@@ -449,13 +498,12 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
             if (threadIdx.x == 0) P.subtick(PROF_ICM_UNION);
             const int root = (algo == ENGINE_ICM_UNION_FIND) ? uf_find(vl, seed) : vl[seed];
             // mark the cluster C (d = 2) and count it
-            for (int u = team.tr; u < n; u += team.ts) {
-                if (!d[u]) continue;
+            for_overlap([&](int u) {
                 const int lu = (algo == ENGINE_ICM_UNION_FIND) ? uf_find(vl, u) : vl[u];
-                if (lu != root) continue;
+                if (lu != root) return;
                 d[u] = 2;
                 csize++;
-            }
+            });
             {
                 unsigned long long m1 = ~0ull, m2 = ~0ull;
                 long long none = 0;
@@ -472,12 +520,12 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
         swapped = (!REPLAY && csize * 2 > cnt) ? 1 : 0;
         const uint8_t fmark = swapped ? 1 : 2;
         const long long fsize = swapped ? cnt - csize : csize;
-        for (int u = team.tr; u < n; u += team.ts) {
-            if (d[u] != fmark) continue;
+        for_overlap([&](int u) {
+            if (d[u] != fmark) return;
             const int hu = D.has_h ? B.h[u] : 0;
             if (locA) { const int sa = sA[u]; sA[u] = (int8_t)-sa; dEa -= 2 * sa * hu; }
             if (locB) { const int sb = sB[u]; sB[u] = (int8_t)-sb; dEb -= 2 * sb * hu; }
-        }
+        });
         team.sync();
         if (BLOCK && fsize * 4 > (long long)n) {
             // a large cluster: fields and energies from scratch (gathers, no
@@ -507,8 +555,8 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
         } else {
             // a small cluster: push the field changes to the neighbours and
             // take the energy change from the edges leaving the cluster
-            for (int u = team.tr; u < n; u += team.ts) {
-                if (d[u] != fmark) continue;
+            for_overlap([&](int u) {
+                if (d[u] != fmark) return;
                 const int sa = locA ? -sA[u] : 0, sb = locB ? -sB[u] : 0;   // spins before the flip
                 const int e1 = B.row[u + 1];
 #pragma unroll 4
@@ -524,7 +572,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                         if (locB) dEb -= 2 * J * sb * sv;
                     }
                 }
-            }
+            });
         }
         team.sync();
     }
@@ -534,6 +582,10 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
             if (locA) B.E[rA] += dEa;
             if (locB && cnt > 0) B.E[rB] += dEb;
         }
+    }
+    if (BLOCK && team.tr == 0) {
+        team.ctl[2] = 0;   // the list counters, for the next pair
+        team.ctl[3] = 0;
     }
     team.sync();
     if (threadIdx.x == 0) P.subtick(PROF_ICM_FLIP);
@@ -1067,6 +1119,14 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
         s_improved[j] = 0;
     }
     if (tid < 8) s_misc[tid] = 0;
+    // the group barrier's generation (it cannot move before this block arrives)
+    unsigned int bar_gen = 0;
+    if (tid == 0 && D.group > 1) bar_gen = *(volatile unsigned int*)(A.bar + 2 * inst + 1);
+    if (tid == 0) {
+        for (int q = 0; q < 3; q++) team_slot_reset(s_team_acc, q);
+        s_team_bc[2] = 0;   // the block team's overlap-list counters
+        s_team_bc[3] = 0;
+    }
     __syncthreads();
     for (int k = tid; k + 1 < nt; k += T) s_dbeta[k] = s_beta[k] - s_beta[k + 1];
     for (int s = tid; s < R; s += T) {
@@ -1091,9 +1151,12 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
     unsigned long long t_step1 = 0;
     for (int ls = 0; ls < A.nsteps; ls++) {
         if (ls == 1 && tid == 0) t_step1 = globaltimer_ns();
-        if (tid == 0) s_misc[3] = *abortf;
-        __syncthreads();
-        if (s_misc[3]) break;
+        if (D.group == 1) {
+            // (a group of blocks sees an abort in its barrier)
+            if (tid == 0) s_misc[3] = *abortf;
+            __syncthreads();
+            if (s_misc[3]) break;
+        }
         const unsigned long long step = A.step0 + (unsigned long long)ls;
         const int parity = (int)(step & 1ull);
         if (A.phase_mask & PHASE_SWEEP) {
@@ -1131,7 +1194,7 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
                 const long long base = parity * A.spins_pub_half + D.spin_off + (long long)B.r0 * npad;
                 for (int idx = tid; idx < rpc * npad; idx += T) A.spins_pub[base + idx] = B.spin[idx];
             }
-            if (!group_barrier(A.bar + 2 * inst, (unsigned)D.group, abortf, A.status)) break;
+            if (!group_barrier(A.bar + 2 * inst, (unsigned)D.group, abortf, A.status, bar_gen)) break;
             for (int r = tid; r < R; r += T)
                 if (r < B.r0 || r >= B.r0 + rpc) B.E[r] = ld_cg(A.energy_pub + parity * A.energy_pub_half + D.rep_off + r);
             __syncthreads();
@@ -1181,7 +1244,7 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
             // the instance is configured with one team (large instances: a
             // pair per block-wide team, in sequence, beats a pair per warp)
             if (BLOCKTEAM || D.teams == 1) {
-                Team<true> team{tid, T, s_team_acc, s_team_bc};
+                const Team<true> team{tid, T, s_team_acc, s_team_bc};
                 const IcmScratch X = icm_scratch(s_icm, npad);
                 for (int j = 0; j < rpc; j++) {
                     const int sl = (int)B.rslot[j], c = sl / nt, k = sl - c * nt, kk = nt - 1 - k;
@@ -1210,6 +1273,10 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
                 }
             }
             __syncthreads();
+            // the block team's reduction slots back to the identity (the
+            // next step's barriers publish it)
+            if (tid == 0)
+                for (int q = 0; q < 3; q++) team_slot_reset(s_team_acc, q);
         }
         P.tick(PROF_ICM);
     }

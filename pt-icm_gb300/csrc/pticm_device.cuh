@@ -173,29 +173,48 @@ __device__ __forceinline__ long long ld_cg(const long long* p) { return __ldcg(p
 __device__ __forceinline__ int8_t ld_cg(const int8_t* p) { return (int8_t)__ldcg((const signed char*)p); }
 
 // -------------------------------------------------------- group barrier
-// A sense-counting barrier over `nblocks` co-resident blocks (guaranteed by
-// a cooperative launch).  Block arrival is counted in bar[0]; the last
-// arriver bumps the generation in bar[1].  Waits are bounded: after
-// kWaitLimitNs, or when another block has raised `abort`, the barrier
-// records the failure and returns false.  Callers return when it fails.
-__device__ __forceinline__ bool group_barrier(unsigned int* bar, unsigned int nblocks,
-                                              volatile int* abort_flag, DevStatus* st) {
+__device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned int atom_add_acq_rel_gpu(unsigned int* p, unsigned int x) {
+    unsigned int old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(x) : "memory");
+    return old;
+}
+
+__device__ __forceinline__ void red_add_release_gpu(unsigned int* p, unsigned int x) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(x) : "memory");
+}
+
+// A counting barrier over `nblocks` co-resident blocks (guaranteed by a
+// cooperative launch).  Arrivals are counted in bar[0] with an acquire-
+// release add (it publishes the block's writes, ordered before it by the
+// block barrier, and acquires the earlier arrivers'); the last arriver
+// resets the count and bumps the generation bar[1] with a release, which
+// the others poll with acquire loads.  `gen` is thread 0's copy of the
+// generation (read when the block joins the group; the generation cannot
+// move before every block has arrived), so arriving costs one atomic.
+// Waits are bounded: after kWaitLimitNs, or when another block has raised
+// `abort`, the barrier records the failure and returns false.  Callers
+// return when it fails.
+__device__ __forceinline__ bool group_barrier(unsigned int* bar, unsigned int nblocks, volatile int* abort_flag,
+                                              DevStatus* st, unsigned int& gen) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned int* gen = bar + 1;
-        const unsigned int g = *gen;
-        __threadfence();
-        const unsigned int arrived = atomicAdd(bar, 1u);
+        const unsigned int g = gen;
+        const unsigned int arrived = atom_add_acq_rel_gpu(bar, 1u);
         int ok = 1;
         if (arrived == nblocks - 1) {
             atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
+            red_add_release_gpu(bar + 1, 1u);
         } else {
             const unsigned long long t0 = globaltimer_ns();
             unsigned int spins = 0;
-            while (*gen == g) {
+            while (ld_acquire_gpu(bar + 1) == g) {
                 if (*abort_flag) { ok = 0; break; }
                 if ((++spins & 63u) == 0 && globaltimer_ns() - t0 > kWaitLimitNs) {
                     dev_fail(st, abort_flag, DEV_BARRIER_TIMEOUT, 1, blockIdx.x, g);
@@ -205,7 +224,7 @@ __device__ __forceinline__ bool group_barrier(unsigned int* bar, unsigned int nb
                 __nanosleep(32);
             }
         }
-        __threadfence();
+        gen = g + 1u;
         s_ok = ok;
     }
     __syncthreads();

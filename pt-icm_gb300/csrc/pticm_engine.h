@@ -170,6 +170,14 @@ inline constexpr uint32_t icm_team_bytes(int32_t n_pad) {
     return (uint32_t)((((uint64_t)n_pad * 5 + 4 * (((uint64_t)n_pad + 31) / 32)) + 15) & ~15ull);
 }
 
+// ICM scratch of a block: `teams` warp teams of icm_team_bytes each, or one
+// block-wide team, which also lists the overlap sites (n_pad ints after its
+// team scratch).
+inline constexpr uint64_t icm_block_bytes(int32_t teams, int32_t n_pad) {
+    return teams == 1 ? (uint64_t)icm_team_bytes(n_pad) + 4ull * (uint64_t)n_pad
+                      : (uint64_t)teams * icm_team_bytes(n_pad);
+}
+
 enum PhaseBits : int32_t { PHASE_SWEEP = 1, PHASE_EXCHANGE = 2, PHASE_ICM = 4 };
 
 // Phase timers: cycles spent per block in sweep, publish+barrier, exchange

@@ -132,7 +132,7 @@ void PlanDims::add(const InstanceDesc& D, bool stage_this, int teams_of_instance
     rpc = std::max(rpc, (uint64_t)D.rpc);
     nt = std::max(nt, (uint64_t)D.nt);
     chains_m = std::max(chains_m, (uint64_t)D.chains * m);
-    icm_bytes = std::max(icm_bytes, (uint64_t)teams_of_instance * icm_team_bytes(D.n_pad));
+    icm_bytes = std::max(icm_bytes, icm_block_bytes(teams_of_instance, D.n_pad));
     teams = std::max(teams, teams_of_instance);
     max_n_pad = std::max(max_n_pad, (uint64_t)D.n_pad);
     max_kmax = std::max(max_kmax, (uint64_t)D.kmax);
@@ -428,7 +428,7 @@ int configure(pticm_ctx* c, bool replay) {
     c->plan = cfg.plan;
     finish_desc(c->desc, c->P, c->o, cfg);
     if (cfg.state_global || cfg.field_gather) {
-        c->icm_stride = (long long)cfg.teams * icm_team_bytes(c->desc.n_pad);
+        c->icm_stride = (long long)icm_block_bytes(cfg.teams, c->desc.n_pad);
         const size_t want = (size_t)cfg.group * (size_t)c->icm_stride;
         if (c->d_icm_pool.n != want) CK(c->d_icm_pool.alloc(want));
     }

@@ -219,9 +219,11 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
     }
     long long cnt = 0, hs = 0;
     unsigned long long kd = ~0ull, ke = ~0ull;
+    const int algo = D.icm_algo;
     auto overlap_site = [&](int i, int8_t a, int8_t b) {
         const bool di = a != b;
         d[i] = di;
+        if (algo == ENGINE_ICM_UNION_FIND) X.queue[i] = i;   // union-find parents
         cnt += di;
         if (!REPLAY) {
             const unsigned long long key = (mix64(r64 + 0x9E3779B97F4A7C15ull * (unsigned long long)(i + 1)) &
@@ -322,7 +324,6 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
         }
     }
     if (threadIdx.x == 0) P.subtick(PROF_ICM_SEED);
-    const int algo = D.icm_algo;
     bool absolute = false;   // energies set from scratch (large flipped sets)
     int swapped = 0;         // the flipped set was D\C (the chains hold each other's result)
     if (cnt > 0) {
@@ -384,10 +385,11 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
             int* lab = X.queue;
             volatile int* vl = lab;
             bool ok = true;
-            if (algo == ENGINE_ICM_UNION_FIND) for_overlap([&](int u) { lab[u] = u; });
-            else
+            // (union-find parents were set with the overlap)
+            if (algo != ENGINE_ICM_UNION_FIND) {
                 for (int i = team.tr; i < n; i += team.ts) lab[i] = d[i] ? i : n;
-            team.sync();
+                team.sync();
+            }
             if (algo == ENGINE_ICM_UNION_FIND) {
                 // Afforest (Sutton, Ben-Nun, Barak, IPDPS 2018): in two
                 // rounds, link every overlap site to its r-th overlap

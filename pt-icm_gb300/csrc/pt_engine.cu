@@ -420,21 +420,26 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                     team.sync();
                 }
                 if (team.tr < 32) {
-                    // vote over 32 sampled overlap sites (one warp)
-                    // each lane samples the first overlap site in a 32-byte
-                    // window of the flags (eight independent word loads; the
-                    // flags start on 16 bytes, bytes from n on are masked)
+                    // vote over 32 sampled overlap sites (one warp): a block
+                    // team samples its overlap list; in a warp team each lane
+                    // takes the first overlap site in a 32-byte window of the
+                    // flags (eight independent word loads; the flags start on
+                    // 16 bytes, bytes from n on are masked)
                     int cand = -1;
-                    const int w0 = (int)(((long long)team.tr * n) >> 7);
-                    uint32_t fw[8];
+                    if (BLOCK) {
+                        cand = vl[lst[l0 + (int)(((long long)team.tr * llen) >> 5)]];
+                    } else {
+                        const int w0 = (int)(((long long)team.tr * n) >> 7);
+                        uint32_t fw[8];
 #pragma unroll
-                    for (int j = 0; j < 8; j++)
-                        fw[j] = 4 * (w0 + j) < n ? reinterpret_cast<const uint32_t*>(d)[w0 + j] : 0u;
-                    for (int j = 0; j < 8 && cand < 0; j++)
-                        for (int b = 0; b < 4; b++) {
-                            const int i = 4 * (w0 + j) + b;
-                            if (i < n && ((fw[j] >> (8 * b)) & 0xffu)) { cand = vl[i]; break; }
-                        }
+                        for (int j = 0; j < 8; j++)
+                            fw[j] = 4 * (w0 + j) < n ? reinterpret_cast<const uint32_t*>(d)[w0 + j] : 0u;
+                        for (int j = 0; j < 8 && cand < 0; j++)
+                            for (int b = 0; b < 4; b++) {
+                                const int i = 4 * (w0 + j) + b;
+                                if (i < n && ((fw[j] >> (8 * b)) & 0xffu)) { cand = vl[i]; break; }
+                            }
+                    }
                     const unsigned grp = __match_any_sync(0xffffffffu, cand);
                     int votes = cand >= 0 ? __popc(grp) : 0, best = cand;
                     for (int o = 16; o > 0; o >>= 1) {
@@ -522,16 +527,15 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
         swapped = (!REPLAY && csize * 2 > cnt) ? 1 : 0;
         const uint8_t fmark = swapped ? 1 : 2;
         const long long fsize = swapped ? cnt - csize : csize;
-        for_overlap([&](int u) {
-            if (d[u] != fmark) return;
-            const int hu = D.has_h ? B.h[u] : 0;
-            if (locA) { const int sa = sA[u]; sA[u] = (int8_t)-sa; dEa -= 2 * sa * hu; }
-            if (locB) { const int sb = sB[u]; sB[u] = (int8_t)-sb; dEb -= 2 * sb * hu; }
-        });
-        team.sync();
         if (BLOCK && fsize * 4 > (long long)n) {
-            // a large cluster: fields and energies from scratch (gathers, no
-            // atomics; the cost does not grow with the cluster)
+            // a large cluster: flip, then fields and energies from scratch
+            // (gathers, no atomics; the cost does not grow with the cluster)
+            for_overlap([&](int u) {
+                if (d[u] != fmark) return;
+                if (locA) sA[u] = (int8_t)-sA[u];
+                if (locB) sB[u] = (int8_t)-sB[u];
+            });
+            team.sync();
             long long eA = 0, eB = 0;
             for (int i = team.tr; i < n; i += team.ts) {
                 int fa = 0, fb = 0;
@@ -555,11 +559,17 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
             }
             absolute = true;
         } else {
-            // a small cluster: push the field changes to the neighbours and
-            // take the energy change from the edges leaving the cluster
+            // a small cluster, flipped and pushed in one pass: each flipped
+            // site sends its field change to its neighbours, and the energy
+            // changes by the edges leaving the flipped set F.  F is a union
+            // of overlap components, so a neighbour outside F is outside the
+            // overlap (equal in A and B) and keeps its spin during the pass.
             for_overlap([&](int u) {
                 if (d[u] != fmark) return;
-                const int sa = locA ? -sA[u] : 0, sb = locB ? -sB[u] : 0;   // spins before the flip
+                const int hu = D.has_h ? B.h[u] : 0;
+                int sa = 0, sb = 0;   // spins before the flip
+                if (locA) { sa = sA[u]; sA[u] = (int8_t)-sa; dEa -= 2 * sa * hu; }
+                if (locB) { sb = sB[u]; sB[u] = (int8_t)-sb; dEb -= 2 * sb * hu; }
                 const int e1 = B.row[u + 1];
 #pragma unroll 4
                 for (int a = B.row[u]; a < e1; a++) {

@@ -161,6 +161,16 @@ PTICM_API int pticm_get_best(pticm_ctx* c, double* energy, uint64_t* sweep, uint
  * of each replica.  Any pointer may be NULL. */
 PTICM_API int pticm_get_replicas(pticm_ctx* c, uint8_t* states, int64_t* energy, int32_t* fields, uint32_t* slot_of_replica);
 
+/* Checkpoint of the PT state of a context: replicas, fields, energies, the
+ * ladder, the slot map, the exchange order and cursor, best states, the
+ * flip and swap counters, the step count (which keys every random stream)
+ * and, when enabled, the energy histograms.  A context created from the same
+ * problem with the same options and loaded from it continues bit for bit as
+ * the uninterrupted run.  The reference has no checkpointing (a run is one
+ * process from src/main.cc to the report). */
+PTICM_API int pticm_checkpoint_save(pticm_ctx* c, const char* path);
+PTICM_API int pticm_checkpoint_load(pticm_ctx* c, const char* path);
+
 /* Ladder and slot -> replica map (beta_indices of src/replica_exchange.cc). */
 PTICM_API int pticm_get_ladder(pticm_ctx* c, double* beta, uint32_t* slot_to_replica, uint32_t* nc);
 

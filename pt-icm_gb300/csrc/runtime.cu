@@ -1285,6 +1285,175 @@ int pticm_cae_ladder(const pticm_problem* p, uint64_t seed, double T0, double T1
     return PTICM_OK;
 }
 
+// ------------------------------------------------------------ checkpoints
+// File: "PTICMCKP", u32 version, u32 0; u64 header words (problem and option
+// identity, counters); nc; the ladder; the histogram range; then each device
+// array as u64 byte count + bytes, in a fixed order.
+}  // extern "C"
+
+namespace {
+
+constexpr uint32_t kCkptVersion = 1;
+
+struct CkptFile {
+    FILE* f = nullptr;
+    bool ok = true;
+    ~CkptFile() {
+        if (f) fclose(f);
+    }
+    void put(const void* p, size_t n) { ok = ok && fwrite(p, 1, n, f) == n; }
+    void get(void* p, size_t n) { ok = ok && fread(p, 1, n, f) == n; }
+    template <class T>
+    void put_val(T v) { put(&v, sizeof v); }
+    template <class T>
+    T get_val() {
+        T v{};
+        get(&v, sizeof v);
+        return v;
+    }
+};
+
+// FNV-1a over the problem's size, adjacency, couplings and linear terms.
+uint64_t problem_fingerprint(const HostProblem& P) {
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](const void* p, size_t n) {
+        const unsigned char* b = static_cast<const unsigned char*>(p);
+        for (size_t i = 0; i < n; i++) h = (h ^ b[i]) * 1099511628211ull;
+    };
+    mix(&P.n, sizeof P.n);
+    mix(P.row.data(), P.row.size() * sizeof(int64_t));
+    mix(P.col.data(), P.col.size() * sizeof(int32_t));
+    mix(P.w.data(), P.w.size() * sizeof(int32_t));
+    mix(P.h.data(), P.h.size() * sizeof(int32_t));
+    return h;
+}
+
+// the identity a checkpoint must share with the context it is loaded into
+std::vector<uint64_t> ckpt_identity(const pticm_ctx* c) {
+    return {(uint64_t)c->P.n, (uint64_t)c->P.col.size(), (uint64_t)c->R,       (uint64_t)c->nt,
+            (uint64_t)c->C,   c->o.seed,                  (uint64_t)c->o.sweeps, (uint64_t)c->o.icm,
+            (uint64_t)c->o.exchange, (uint64_t)c->o.best_per_phase, problem_fingerprint(c->P)};
+}
+
+template <class T>
+int ckpt_dump(CkptFile& F, const DArr<T>& a) {
+    std::vector<T> v;
+    CK(a.download(v));
+    F.put_val<uint64_t>(v.size() * sizeof(T));
+    F.put(v.data(), v.size() * sizeof(T));
+    return PTICM_OK;
+}
+
+template <class T>
+int ckpt_restore(CkptFile& F, DArr<T>& a, const char* what) {
+    const uint64_t bytes = F.get_val<uint64_t>();
+    if (!F.ok || bytes != a.n * sizeof(T))
+        return fail(PTICM_ERR_INVALID, std::string("checkpoint: ") + what + " does not match the context");
+    std::vector<T> v(a.n);
+    F.get(v.data(), bytes);
+    if (!F.ok) return fail(PTICM_ERR_IO, std::string("checkpoint: short read in ") + what);
+    if (bytes) CK(cudaMemcpy(a.p, v.data(), bytes, cudaMemcpyHostToDevice));
+    return PTICM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pticm_checkpoint_save(pticm_ctx* c, const char* path) {
+    if (!c || !path) return fail(PTICM_ERR_INVALID, "null argument");
+    if (!c->ladder_set || !c->states_set) return fail(PTICM_ERR_INVALID, "nothing to save: set a ladder and states");
+    CK(cudaStreamSynchronize(c->stream));
+    CkptFile F;
+    F.f = fopen(path, "wb");
+    if (!F.f) return fail(PTICM_ERR_IO, std::string("cannot write ") + path);
+    F.put("PTICMCKP", 8);
+    F.put_val<uint32_t>(kCkptVersion);
+    F.put_val<uint32_t>(0);
+    for (uint64_t v : ckpt_identity(c)) F.put_val<uint64_t>(v);
+    F.put_val<uint64_t>((uint64_t)c->desc.n_pad);
+    F.put_val<uint64_t>(c->steps_done);
+    F.put_val<uint64_t>(c->attempts);
+    F.put_val<int64_t>(c->nc);
+    F.put(c->beta.data(), c->beta.size() * sizeof(double));
+    const bool hist = c->d_hist.p != nullptr;
+    F.put_val<uint64_t>(hist ? c->hist_from : 0);
+    F.put_val<int64_t>(hist ? c->hist_lo : 0);
+    F.put_val<int64_t>(hist ? c->hist_nbins : 0);
+    int rc = PTICM_OK;
+    if (!rc) rc = ckpt_dump(F, c->d_spins);
+    if (!rc) rc = ckpt_dump(F, c->d_fields);
+    if (!rc) rc = ckpt_dump(F, c->d_E);
+    if (!rc) rc = ckpt_dump(F, c->d_bestE);
+    if (!rc) rc = ckpt_dump(F, c->d_best_state);
+    if (!rc) rc = ckpt_dump(F, c->d_flips);
+    if (!rc) rc = ckpt_dump(F, c->d_bestSweep);
+    if (!rc) rc = ckpt_dump(F, c->d_att);
+    if (!rc) rc = ckpt_dump(F, c->d_succ);
+    if (!rc) rc = ckpt_dump(F, c->d_slot);
+    if (!rc) rc = ckpt_dump(F, c->d_order);
+    if (!rc) rc = ckpt_dump(F, c->d_cursor);
+    if (!rc && hist) rc = ckpt_dump(F, c->d_hist);
+    if (!rc && hist) rc = ckpt_dump(F, c->d_obs);
+    if (rc) return rc;
+    if (!F.ok) return fail(PTICM_ERR_IO, std::string("short write to ") + path);
+    return PTICM_OK;
+}
+
+int pticm_checkpoint_load(pticm_ctx* c, const char* path) {
+    if (!c || !path) return fail(PTICM_ERR_INVALID, "null argument");
+    CkptFile F;
+    F.f = fopen(path, "rb");
+    if (!F.f) return fail(PTICM_ERR_IO, std::string("cannot read ") + path);
+    char magic[8] = {};
+    F.get(magic, 8);
+    const uint32_t version = F.get_val<uint32_t>();
+    F.get_val<uint32_t>();
+    if (!F.ok || memcmp(magic, "PTICMCKP", 8) != 0 || version != kCkptVersion)
+        return fail(PTICM_ERR_INVALID, "not a PT-ICM checkpoint of this version");
+    const std::vector<uint64_t> want = ckpt_identity(c);
+    for (size_t k = 0; k < want.size(); k++)
+        if (F.get_val<uint64_t>() != want[k] || !F.ok)
+            return fail(PTICM_ERR_INVALID,
+                        "checkpoint was written for another problem, ladder size or option set");
+    if (int rc = configure(c, false)) return rc;
+    if (F.get_val<uint64_t>() != (uint64_t)c->desc.n_pad)
+        return fail(PTICM_ERR_INVALID, "checkpoint site padding differs");
+    const uint64_t steps = F.get_val<uint64_t>(), attempts = F.get_val<uint64_t>();
+    const int64_t nc = F.get_val<int64_t>();
+    std::vector<double> beta((size_t)c->nt);
+    F.get(beta.data(), beta.size() * sizeof(double));
+    const uint64_t hist_from = F.get_val<uint64_t>();
+    const int64_t hist_lo = F.get_val<int64_t>(), hist_nbins = F.get_val<int64_t>();
+    if (!F.ok) return fail(PTICM_ERR_IO, "checkpoint header is truncated");
+    if (int rc = pticm_set_ladder(c, beta.data(), (uint32_t)c->nt, (int32_t)nc)) return rc;
+    if (hist_nbins > 0) {
+        if (int rc = pticm_enable_energy_histograms(c, hist_from)) return rc;
+        if (c->hist_lo != hist_lo || c->hist_nbins != hist_nbins)
+            return fail(PTICM_ERR_INVALID, "checkpoint histogram range differs");
+    }
+    int rc = PTICM_OK;
+    if (!rc) rc = ckpt_restore(F, c->d_spins, "spins");
+    if (!rc) rc = ckpt_restore(F, c->d_fields, "fields");
+    if (!rc) rc = ckpt_restore(F, c->d_E, "energies");
+    if (!rc) rc = ckpt_restore(F, c->d_bestE, "best energies");
+    if (!rc) rc = ckpt_restore(F, c->d_best_state, "best states");
+    if (!rc) rc = ckpt_restore(F, c->d_flips, "flip counts");
+    if (!rc) rc = ckpt_restore(F, c->d_bestSweep, "best sweeps");
+    if (!rc) rc = ckpt_restore(F, c->d_att, "swap attempts");
+    if (!rc) rc = ckpt_restore(F, c->d_succ, "swap successes");
+    if (!rc) rc = ckpt_restore(F, c->d_slot, "slot map");
+    if (!rc) rc = ckpt_restore(F, c->d_order, "exchange order");
+    if (!rc) rc = ckpt_restore(F, c->d_cursor, "exchange cursor");
+    if (!rc && hist_nbins > 0) rc = ckpt_restore(F, c->d_hist, "histograms");
+    if (!rc && hist_nbins > 0) rc = ckpt_restore(F, c->d_obs, "observables");
+    if (rc) return rc;
+    c->steps_done = steps;
+    c->attempts = attempts;
+    c->states_set = true;
+    return PTICM_OK;
+}
+
 int pticm_philox_probe(const uint32_t* ctr, const uint32_t* key, uint32_t* out, int count) {
     if (!ctr || !key || !out || count <= 0) return fail(PTICM_ERR_INVALID, "invalid arguments");
     if (int rc = check_device()) return rc;

@@ -40,7 +40,13 @@ void usage() {
         "  --icm-algo auto|bfs|union-find|label-prop\n"
         "  --sort-ladder               sort a --preprocess or learned ladder ascending (ICM on the coldest)\n"
         "  --learned-ladder FILE       constant-acceptance ladder from a trained surrogate network (no pilot\n"
-        "                              run); checked by a short PT run, multihistogram ladder as fallback\n");
+        "                              run); checked by a short PT run, multihistogram ladder as fallback\n"
+        "  --checkpoint FILE           write the PT state after the run (resumable)\n"
+        "  --resume FILE               continue the run a checkpoint holds (same problem and options)\n"
+        "Folder mode (the reference's unreachable src/main.cc:149-207), instead of --problem:\n"
+        "  --folder DIR                run every problem file of DIR\n"
+        "  --restarts N                runs per problem (default 1)\n"
+        "  --csv FILE                  one row per run, the reference's columns (default: stdout)\n");
 }
 
 }  // namespace
@@ -49,7 +55,8 @@ int main(int argc, char** argv) {
     pticm::PTWorker w;
     pticm::Parameters& P = w.params;
     P.seed = (uint64_t)time(NULL);
-    std::string problem_path;
+    std::string problem_path, folder, csv;
+    size_t restarts = 1;
     bool help = argc <= 1;
     try {
         for (int i = 1; i < argc; i++) {
@@ -92,9 +99,14 @@ int main(int argc, char** argv) {
                 else throw std::runtime_error("unknown --icm-algo " + v);
             } else if (a == "--sort-ladder") P.sort_ladder = true;
             else if (a == "--learned-ladder") P.learned_ladder = next();
+            else if (a == "--resume") P.resume = next();
+            else if (a == "--checkpoint") P.checkpoint = next();
+            else if (a == "--folder") folder = next();
+            else if (a == "--csv") csv = next();
+            else if (a == "--restarts") restarts = std::stoull(next());
             else throw std::runtime_error("unknown argument " + a);
         }
-        if (!help && problem_path.empty()) throw std::runtime_error("--problem is required");
+        if (!help && problem_path.empty() && folder.empty()) throw std::runtime_error("--problem is required");
     } catch (const std::exception& e) {
         std::cout << e.what() << std::endl;
         usage();
@@ -117,7 +129,17 @@ int main(int argc, char** argv) {
     std::cout << "Log Data: " << P.log_data << std::endl;
     std::cout << "ICM: " << P.icm << std::endl;
     std::cout << "Verbosity: " << P.verbosity << std::endl;
-    std::cout << problem_path << std::endl;
+    std::cout << (folder.empty() ? problem_path : folder) << std::endl;
+    if (!folder.empty()) {
+        try {
+            const size_t rows = pticm::solve_folder(w, folder, csv, restarts);
+            if (!csv.empty()) std::cout << rows << " runs written to " << csv << std::endl;
+        } catch (const std::exception& e) {
+            std::fprintf(stderr, "pt_icm: %s\n", e.what());
+            return 1;
+        }
+        return 0;
+    }
     try {
         double best_ene = 0;
         size_t flips = 0;

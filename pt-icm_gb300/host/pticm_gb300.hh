@@ -46,6 +46,8 @@ struct Parameters {
     uint32_t icm_algo = 0;            // 0 automatic, 1 BFS, 2 union-find, 3 label propagation
     bool sort_ladder = false;         // sort a --preprocess ladder ascending (ICM on the coldest)
     std::string learned_ladder;       // surrogate network file: learned ladder (multihistogram fallback)
+    std::string resume;               // checkpoint to continue from (pticm_checkpoint_load)
+    std::string checkpoint;           // checkpoint written after the run (pticm_checkpoint_save)
 };
 
 // include/problem.hh:7-98
@@ -104,12 +106,22 @@ struct PTWorker {
 // include/solver.hh:6 -- the whole PT-ICM run, printing the reference's report
 void solve(PTWorker& w, std::string& problem_path, double& best_ene, size_t& flips, StateVector& best_state);
 
+// The folder mode of src/main.cc:149-207 (unreachable there: its parser never
+// sets the folder): every problem file of `folder`, `restarts` runs each, one
+// CSV row per run with the reference's columns.  All runs with ladders of one
+// length share one batched launch; returns the rows written.
+size_t solve_folder(PTWorker& w, const std::string& folder, const std::string& csv_path, size_t restarts);
+
 // src/mpi_utils.cc:6-22
 void beta_linspace(double* temps, double T0, double T1, uint64_t num_temp, bool inverse);
 
 // include/utils.hh:91-93 (src/cae_estimator.cc:295-428): fills w.beta_values
 // with the multihistogram constant-acceptance ladder and sets w.params.Nt
 void get_beta(PTWorker& w, double estep, double step_size, double r, size_t num_samples);
+
+// The ladder of src/initialization.cc:103-157 (linspace, --preprocess, or the
+// learned ladder) into w.beta_values, w.params.Nt set to its length
+void choose_ladder(PTWorker& w);
 
 // src/initialization.cc:103-191 / 63-100: ladder, Nc, replicas, exchange state
 void initialize_temperatures(PTWorker& w);

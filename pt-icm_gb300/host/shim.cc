@@ -129,7 +129,7 @@ void learned_beta(PTWorker& w, double r) {
                     info.fallback ? "multihistogram fallback" : "accepted", info.mean_deviation, info.rounds);
 }
 
-void initialize_temperatures(PTWorker& w) {
+void choose_ladder(PTWorker& w) {
     w.characteristic_scale = w.p.get_char_scale();
     if (!w.params.learned_ladder.empty()) {
         learned_beta(w, 0.4);
@@ -141,6 +141,10 @@ void initialize_temperatures(PTWorker& w) {
         w.beta_values.assign(w.params.Nt, 0.0);
         beta_linspace(w.beta_values.data(), w.params.T0, w.params.T1, w.params.Nt, w.params.inverse);
     }
+}
+
+void initialize_temperatures(PTWorker& w) {
+    choose_ladder(w);
     pticm_opts o;
     pticm_opts_default(&o);
     o.seed = w.params.seed;
@@ -207,10 +211,26 @@ void solve(PTWorker& w, std::string& problem_path, double& best_ene, size_t& fli
     const auto t0 = std::chrono::steady_clock::now();
     w.p = Problem(problem_path, w.params.seed, w.params.burn_in);
     initialize_temperatures(w);
-    initialize_replicas(w);
+    bool have_hist = false;
+    if (!w.params.resume.empty()) {
+        // continue a checkpointed run: its ladder, replicas, counters and
+        // step count replace the fresh ones (a context of the same problem
+        // and options is required)
+        check(pticm_checkpoint_load(w.ctx, w.params.resume.c_str()));
+        const size_t nt = (size_t)w.params.Nt;
+        check(pticm_get_ladder(w.ctx, w.beta_values.data(), nullptr, nullptr));
+        for (uint32_t c = 1; c < w.params.chains; c++)
+            std::copy(w.beta_values.begin(), w.beta_values.begin() + nt, w.beta_values.begin() + c * nt);
+        int64_t lo = 0;
+        uint64_t nb = 0;
+        have_hist = pticm_get_energy_histograms(w.ctx, nullptr, &lo, &nb) == PTICM_OK;
+    } else {
+        initialize_replicas(w);
+    }
     // --log: per-temperature observables from the steps after the burn-in
-    if (w.params.log_data) check(pticm_enable_energy_histograms(w.ctx, w.params.burn_in));
+    if (w.params.log_data && !have_hist) check(pticm_enable_energy_histograms(w.ctx, w.params.burn_in));
     check(pticm_run(w.ctx, w.params.pts, PTICM_PHASE_ALL));
+    if (!w.params.checkpoint.empty()) check(pticm_checkpoint_save(w.ctx, w.params.checkpoint.c_str()));
     size_t best_sweep = 0;
     gather_best_energy_values(w, best_ene, best_sweep, best_state);
     flips = (size_t)get_flips(w);

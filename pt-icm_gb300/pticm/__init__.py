@@ -90,6 +90,8 @@ def lib():
         "pticm_get_replicas": [P, P, P, P, P],
         "pticm_get_ladder": [P, P, P, P],
         "pticm_verify": [P, P],
+        "pticm_checkpoint_save": [P, C.c_char_p],
+        "pticm_checkpoint_load": [P, C.c_char_p],
         "pticm_replay": [P, C.POINTER(Trace)],
         "pticm_philox_probe": [P, P, P, C.c_int],
         "pticm_set_profiling": [P, C.c_int],
@@ -371,6 +373,15 @@ class Context:
         mm = C.c_uint64()
         _check(lib().pticm_verify(self._h, C.byref(mm)))
         return mm.value
+
+    def checkpoint_save(self, path: str):
+        """Write the PT state (replicas, ladder, slot map, counters, step)."""
+        _check(lib().pticm_checkpoint_save(self._h, os.fsencode(path)))
+
+    def checkpoint_load(self, path: str):
+        """Restore a checkpoint written by a context of the same problem and
+        options; the run continues bit for bit."""
+        _check(lib().pticm_checkpoint_load(self._h, os.fsencode(path)))
 
     def replay(self, trace: dict, pt_steps: int):
         """Run the reference's sequential algorithm from a recorded trace

@@ -71,3 +71,50 @@ def test_cli_log_prints_observables():
     for T, C, X, u, m in rows:
         assert 0.5 - 1e-9 <= T <= 3.0 + 1e-9
         assert C >= 0 and X >= 0 and -2.0 <= u <= 0.0 and abs(m) <= 1.0
+
+
+def test_cli_checkpoint_resume(tmp_path):
+    """--checkpoint after k steps, --resume for k more equals one 2k-step run."""
+    path = os.path.join(G, "pmL10.gset")
+    common = ["-p", path, "-s", "9", "-r", "8", "--icm", "-T0", "0.5", "-T1", "3.0"]
+    ck = str(tmp_path / "half.ckpt")
+    _run(*common, "--pts", "150", "--checkpoint", ck)
+    resumed = _parse(_run(*common, "--pts", "150", "--resume", ck))
+    whole = _parse(_run(*common, "--pts", "300"))
+    for key in ("swap_attempts", "swap_successes", "best_energy", "best_state_sweep", "num_of_flips",
+                "num_of_swaps", "best_state"):
+        assert resumed[key] == whole[key], key
+
+
+def test_cli_folder_csv(tmp_path):
+    """The folder mode: one CSV row per (problem, restart) with the
+    reference's columns; each row's energy and cut are those of its state."""
+    import csv
+    import shutil
+    d = tmp_path / "problems"
+    d.mkdir()
+    names = ["pmL6.gset", "pmL10.gset", "rnd60_pm"]
+    for name in names:
+        shutil.copy(os.path.join(G, name), d / name)
+    out = tmp_path / "runs.csv"
+    _run("--folder", str(d), "--csv", str(out), "--restarts", "2", "-s", "5", "-r", "8", "--pts", "300", "--icm",
+         "-T0", "0.5", "-T1", "3.0")
+    with open(out) as f:
+        rows = list(csv.DictReader(f))
+    assert list(rows[0].keys()) == ["problem", "iter", "pts", "replicas", "tlist", "pswap", "icm", "preprocess",
+                                    "burn_in", "inverse", "sweeps", "ene", "state", "cut", "flips"]
+    assert len(rows) == len(names) * 2
+    assert [os.path.basename(r["problem"]) for r in rows] == [n for n in sorted(names) for _ in range(2)]
+    assert [int(r["iter"]) for r in rows] == [0, 1] * len(names)
+    for r in rows:
+        assert int(r["pts"]) == 300 and int(r["replicas"]) == 8 and r["icm"] == "1"
+        tlist = [float(x) for x in r["tlist"][1:-1].split(";")]
+        pswap = [float(x) for x in r["pswap"][1:-1].split(";")]
+        assert len(tlist) == 16 and len(pswap) == 16 and all(0.0 <= p <= 1.0 for p in pswap)
+        assert tlist[0] == pytest.approx(1 / 3.0, rel=1e-5) and tlist[7] == pytest.approx(2.0, rel=1e-5)
+        prob = O.Problem.load(r["problem"], 0)
+        state = [int(c) for c in r["state"]]
+        assert len(state) == prob.n
+        assert float(r["ene"]) == pytest.approx(prob.energy(state), abs=1e-9)
+        assert float(r["cut"]) == pytest.approx(prob.maxcut(state), abs=1e-9)
+        assert int(r["flips"]) > 0

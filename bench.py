@@ -260,9 +260,15 @@ def run_gpu(args):
     value = job_throughput(world, attempts_per_step * args.steps, total_ms)
     mism = ctx.verify()
 
-    # end-to-end through the C ABI from host buffers, per step
+    # end-to-end through the C ABI from host buffers, per step.  The input
+    # states are the warmed-up replicas, each given to the replica that
+    # starts at its temperature, so that the timed steps do the same
+    # (equilibrium) work as the device-timed ones.
+    s_now, _, _, slot_now = ctx.replicas()
+    by_slot = np.empty_like(s_now)
+    by_slot[slot_now] = s_now
     states_host = torch.empty((2 * NT, N_SPINS), dtype=torch.uint8).pin_memory()
-    states_host.copy_(torch.from_numpy(np.random.default_rng(7 + rank).integers(0, 2, size=(2 * NT, N_SPINS), dtype=np.uint8)))
+    states_host.copy_(torch.from_numpy(by_slot))
     src = np.ascontiguousarray(inst.src, np.int32)
     dst = np.ascontiguousarray(inst.dst, np.int32)
     w = np.ascontiguousarray(inst.w, np.float64)
@@ -305,8 +311,8 @@ def run_gpu(args):
                    "wall_s": wall, "verify_mismatches_after": mism},
         "e2e": {"value": e2e_value, "unit": "attempts/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h),
-                "what": "problem upload + ladder + initial states from pinned host memory + "
-                        "1000 PT steps + best state/statistics read back, per step"},
+                "what": "problem upload + ladder + initial states (the warmed-up replicas) from pinned host "
+                        "memory + 1000 PT steps + best state/statistics read back, per step"},
         "gpu_launches": args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": _profiled_traffic(),

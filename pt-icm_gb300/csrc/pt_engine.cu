@@ -38,11 +38,13 @@ __device__ __forceinline__ T* sm_ptr(uint8_t* base, uint32_t off) {
 struct Prof {
     bool on;
     long long mark, sub;
-    long long c[PROF_PHASES];
-    __device__ __forceinline__ void init(bool enable) {
+    long long* c;   // PROF_PHASES counters in shared memory (thread 0 only)
+    __device__ __forceinline__ void init(bool enable, long long* store) {
         on = enable;
+        c = store;
         mark = sub = enable ? clock64() : 0;
-        for (int q = 0; q < PROF_PHASES; q++) c[q] = 0;
+        if (enable)
+            for (int q = 0; q < PROF_PHASES; q++) c[q] = 0;
     }
     __device__ __forceinline__ void tick(int slot) {
         if (on) { const long long t = clock64(); c[slot] += t - mark; mark = t; sub = t; }
@@ -1010,6 +1012,10 @@ __device__ void exchange_replay(const EngineArgs& A, const BlockCtx& B, int ls, 
 template <bool REPLAY, bool BLOCKTEAM>
 __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) {
     extern __shared__ __align__(128) uint8_t smem[];
+    // the job's context and the profiling counters: one copy per block (per-
+    // thread copies of uniform values would live in local memory)
+    __shared__ BlockCtx s_B;
+    __shared__ long long s_prof[PROF_PHASES];
     const SmemPlan& S = A.sm;
     const int tid = threadIdx.x, T = blockDim.x;
     volatile int* abortf = A.abort_flag;
@@ -1021,35 +1027,26 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
     uint32_t bulk_parity = 0;
     const int job_end = A.sched_off[blockIdx.x + 1];
     for (int job = A.sched_off[blockIdx.x]; job < job_end; job++) {
-    BlockCtx B;
     const int inst = A.sched[2 * job];
-    B.D = A.desc[inst];
+    if (tid == 0) {
+        s_B.D = A.desc[inst];
+        s_B.rank = A.sched[2 * job + 1];
+        s_B.r0 = s_B.rank * s_B.D.rpc;
+    }
+    __syncthreads();
+    BlockCtx& B = s_B;
     const InstanceDesc& D = B.D;
-    B.rank = A.sched[2 * job + 1];
-    B.r0 = B.rank * D.rpc;
     const int n = D.n, npad = D.n_pad, R = D.R, nt = D.nt, rpc = D.rpc, kst = D.kmax + 1;
 
     int32_t* s_col = sm_ptr<int32_t>(smem, S.col);
     int32_t* s_h = sm_ptr<int32_t>(smem, S.h);
-    if (S.state_global) {
-        // replicas too large for shared memory work on their master copy
-        B.spin = A.spins + D.spin_off + (long long)B.r0 * D.n_pad;
-        B.field = A.fields + D.spin_off + (long long)B.r0 * D.n_pad;
-    } else {
-        B.spin = sm_ptr<int8_t>(smem, S.spin);
-        B.field = S.field_gather ? nullptr : sm_ptr<int32_t>(smem, S.field);
-    }
     // acceptance thresholds: shared memory, or read through L1 (field_gather)
     uint32_t* s_thr_w = sm_ptr<uint32_t>(smem, S.thr);
     const uint32_t* s_thr = S.field_gather ? A.thr + D.thr_off : s_thr_w;
     double* s_ptab = sm_ptr<double>(smem, S.ptab);
-    B.slot = sm_ptr<uint32_t>(smem, S.slot);
-    B.rslot = sm_ptr<uint32_t>(smem, S.rslot);
-    B.tb = sm_ptr<int32_t>(smem, S.rslot) + rpc;
     uint32_t* s_order = sm_ptr<uint32_t>(smem, S.order);
     double* s_beta = sm_ptr<double>(smem, S.beta);
     double* s_dbeta = sm_ptr<double>(smem, S.dbeta);
-    B.E = sm_ptr<long long>(smem, S.E);
     int* s_dEp = sm_ptr<int>(smem, S.dEp);
     unsigned* s_flp = sm_ptr<unsigned>(smem, S.flp);
     long long* s_bestE = sm_ptr<long long>(smem, S.bestE);
@@ -1070,7 +1067,6 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
 
     const int32_t* g_row = A.row + D.row_off;
     const uint32_t* g_adj = A.adj + D.adj_off;
-    B.h = D.has_h ? s_h : nullptr;
 
     // ---- stage the adjacency (bulk copies) and load the block's state
     bool staged = S.stage_adj && D.stage;
@@ -1093,12 +1089,25 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
             bulk_g2s(s_row, g_row, rb, mbar);
             if (ab) bulk_g2s(s_adj, g_adj, ab, mbar);
         }
-        B.row = s_row;
-        B.adj = s_adj;
-    } else {
-        B.row = g_row;
-        B.adj = g_adj;
     }
+    if (tid == 0) {
+        if (S.state_global) {
+            // replicas too large for shared memory work on their master copy
+            B.spin = A.spins + D.spin_off + (long long)B.r0 * D.n_pad;
+            B.field = A.fields + D.spin_off + (long long)B.r0 * D.n_pad;
+        } else {
+            B.spin = sm_ptr<int8_t>(smem, S.spin);
+            B.field = S.field_gather ? nullptr : sm_ptr<int32_t>(smem, S.field);
+        }
+        B.slot = sm_ptr<uint32_t>(smem, S.slot);
+        B.rslot = sm_ptr<uint32_t>(smem, S.rslot);
+        B.tb = sm_ptr<int32_t>(smem, S.rslot) + rpc;
+        B.E = sm_ptr<long long>(smem, S.E);
+        B.h = D.has_h ? s_h : nullptr;
+        B.row = staged ? sm_ptr<int32_t>(smem, S.row) : g_row;
+        B.adj = staged ? sm_ptr<uint32_t>(smem, S.adj) : g_adj;
+    }
+    __syncthreads();
     for (int i = tid; i <= D.ncolors; i += T) s_col[i] = A.col[D.col_off + i];
     if (D.has_h)
         for (int i = tid; i < n; i += T) s_h[i] = A.hpool[D.h_off + i];
@@ -1157,7 +1166,7 @@ __global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) 
 
     const bool icm_on = (A.phase_mask & PHASE_ICM) && D.nc > 0 && D.chains >= 2;
     Prof P;
-    P.init((A.prof != nullptr) && tid == 0);
+    P.init((A.prof != nullptr) && tid == 0, s_prof);
     const long long t_start = P.mark;
     const bool best_pp = (A.flags & ENGINE_BEST_PER_PHASE) != 0;
     unsigned long long t_step1 = 0;

@@ -244,7 +244,7 @@ int configure_batch(pticm_batch* b) {
     int dev = 0, sms = 0, per_sm = 0;
     BCK(cudaGetDevice(&dev));
     BCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    BCK(engine_max_blocks_per_sm(false, false, b->threads, b->plan.total, &per_sm));
+    BCK(engine_max_blocks_per_sm(false, false, false, b->threads, b->plan.total, &per_sm));
     if (per_sm < 1) return bfail(PTICM_ERR_UNSUPPORTED, "the engine block does not fit on an SM");
     long long total_blocks = 0;
     int gmax = 0;
@@ -336,7 +336,7 @@ int batch_launch(pticm_batch* b, uint64_t step0, int steps, uint32_t phase_mask,
     A.phase_mask = (int)phase_mask;
     A.job_ns = job_ns;
     BCK(cudaEventRecord(b->ev0, b->stream));
-    BCK(launch_engine(A, b->threads, false, false, true, b->stream));
+    BCK(launch_engine(A, b->threads, false, false, false, true, b->stream));
     BCK(cudaEventRecord(b->ev1, b->stream));
     BCK(cudaEventSynchronize(b->ev1));
     float ms = 0.f;

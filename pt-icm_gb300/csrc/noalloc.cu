@@ -239,7 +239,7 @@ extern "C" int pticm_run_noalloc(const pticm_problem* p, const pticm_opts* o, co
         A.nsteps = chunk;
         A.phase_mask = PHASE_SWEEP | PHASE_EXCHANGE | PHASE_ICM;
         NA_CK(cudaMemsetAsync(base + o_bar, 0, 2 * sizeof(unsigned), st));
-        NA_CK(launch_engine(A, cfg.threads, false, cfg.block_team, cfg.group > 1, st));
+        NA_CK(launch_engine(A, cfg.threads, false, cfg.block_team, cfg.narrow, cfg.group > 1, st));
         step += (uint64_t)chunk;
         left -= (uint64_t)chunk;
     }

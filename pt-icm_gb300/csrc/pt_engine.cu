@@ -1009,8 +1009,10 @@ __device__ void exchange_replay(const EngineArgs& A, const BlockCtx& B, int ls, 
 }
 
 // ---------------------------------------------------------------- kernel
-template <bool REPLAY, bool BLOCKTEAM>
-__global__ void __launch_bounds__(1024, 1) pt_engine_kernel(const EngineArgs A) {
+// NARROW: a block team of at most kNarrowThreads threads, one block per SM;
+// the bound leaves each thread 120 registers instead of 64.
+template <bool REPLAY, bool BLOCKTEAM, bool NARROW>
+__global__ void __launch_bounds__(NARROW ? kNarrowThreads : 1024, 1) pt_engine_kernel(const EngineArgs A) {
     extern __shared__ __align__(128) uint8_t smem[];
     // the job's context and the profiling counters: one copy per block (per-
     // thread copies of uniform values would live in local memory)
@@ -1464,12 +1466,16 @@ __global__ void evaluate_kernel(const int32_t* row, const uint32_t* adj, const i
 }
 
 // ------------------------------------------------------------ launchers
-cudaError_t launch_engine(const EngineArgs& A, int threads, bool replay, bool block_team, bool cooperative,
-                          cudaStream_t stream) {
-    void* fn;
-    if (replay) fn = (void*)pt_engine_kernel<true, false>;
-    else if (block_team) fn = (void*)pt_engine_kernel<false, true>;
-    else fn = (void*)pt_engine_kernel<false, false>;
+static void* engine_fn(bool replay, bool block_team, bool narrow) {
+    if (replay) return (void*)pt_engine_kernel<true, false, false>;
+    if (block_team && narrow) return (void*)pt_engine_kernel<false, true, true>;
+    if (block_team) return (void*)pt_engine_kernel<false, true, false>;
+    return (void*)pt_engine_kernel<false, false, false>;
+}
+
+cudaError_t launch_engine(const EngineArgs& A, int threads, bool replay, bool block_team, bool narrow,
+                          bool cooperative, cudaStream_t stream) {
+    void* fn = engine_fn(replay, block_team, narrow);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)A.sm.total);
     if (e != cudaSuccess) return e;
     void* args[] = {(void*)&A};
@@ -1478,11 +1484,12 @@ cudaError_t launch_engine(const EngineArgs& A, int threads, bool replay, bool bl
     return cudaLaunchKernel(fn, dim3(A.n_blocks), dim3(threads), args, A.sm.total, stream);
 }
 
-cudaError_t engine_max_blocks_per_sm(bool replay, bool block_team, int threads, size_t smem, int* out) {
-    const void* fn;
-    if (replay) fn = (const void*)pt_engine_kernel<true, false>;
-    else if (block_team) fn = (const void*)pt_engine_kernel<false, true>;
-    else fn = (const void*)pt_engine_kernel<false, false>;
+cudaError_t engine_max_blocks_per_sm(bool replay, bool block_team, bool narrow, int threads, size_t smem, int* out) {
+    if (narrow && threads > kNarrowThreads) {
+        *out = 0;
+        return cudaSuccess;
+    }
+    const void* fn = engine_fn(replay, block_team, narrow);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, fn, threads, smem);

@@ -25,9 +25,6 @@
 #include "mhist_job.h"
 
 namespace pticm {
-cudaError_t launch_engine(const EngineArgs& A, int threads, bool replay, bool block_team, bool cooperative,
-                          cudaStream_t stream);
-cudaError_t engine_max_blocks_per_sm(bool replay, bool block_team, int threads, size_t smem, int* out);
 cudaError_t launch_recompute(const EngineArgs& A, const int32_t* rep_inst, int total_reps, int write_back,
                              unsigned long long* mismatches, long long* E_out, long long* cut2_out,
                              cudaStream_t stream);
@@ -82,7 +79,7 @@ struct pticm_ctx {
     std::vector<double> beta;
     InstanceDesc desc{};
     int rpc = 0, group = 0, threads = 0, teams = 1;
-    bool block_team = false;
+    bool block_team = false, narrow = false;
     SmemPlan plan{};
     uint64_t steps_done = 0, attempts = 0;
     double last_ms = 0.0;
@@ -237,7 +234,9 @@ int choose_config(const HostProblem& P, const pticm_opts& o, bool replay, Instan
     if (replay) threads = std::min(1024, 32 * std::max(1, std::min(R, 32)));
     if (threads <= 0) {
         if (rpc > 1) threads = 1024;
-        else threads = std::min(1024, std::max(128, ((std::max(max_class, n / 2) + 31) / 32) * 32));
+        // one replica per block: at most the narrow-bound block (on N=2000,
+        // 512 threads at 120 registers beat 1024 threads at 64 by 11 %)
+        else threads = std::min(kNarrowThreads, std::max(128, ((std::max(max_class, n / 2) + 31) / 32) * 32));
     }
     if (threads % 32 != 0 || threads > 1024) {
         msg = "block_threads must be a multiple of 32, at most 1024";
@@ -270,7 +269,7 @@ int choose_config(const HostProblem& P, const pticm_opts& o, bool replay, Instan
                 const SmemPlan p1 = make_plan(d1, false, 1, t, false, false, true);
                 if (p1.total > kSmemLimit) continue;
                 int per_sm = 0;
-                if (engine_max_blocks_per_sm(false, true, t, p1.total, &per_sm) != cudaSuccess) continue;
+                if (engine_max_blocks_per_sm(false, true, false, t, p1.total, &per_sm) != cudaSuccess) continue;
                 if ((int64_t)per_sm * sms < R) continue;
                 rpc = 1;
                 threads = t;
@@ -298,7 +297,7 @@ int choose_config(const HostProblem& P, const pticm_opts& o, bool replay, Instan
                 const SmemPlan p1 = make_plan(d1, false, 1, t, false, true);
                 if (p1.total > kSmemLimit) continue;
                 int per_sm = 0;
-                if (engine_max_blocks_per_sm(false, true, t, p1.total, &per_sm) != cudaSuccess) continue;
+                if (engine_max_blocks_per_sm(false, true, false, t, p1.total, &per_sm) != cudaSuccess) continue;
                 if ((int64_t)per_sm * sms < R) continue;
                 rpc = 1;
                 threads = t;
@@ -324,6 +323,16 @@ int choose_config(const HostProblem& P, const pticm_opts& o, bool replay, Instan
     }
     cfg.state_global = global;
     group = R / rpc;
+    // a block team takes the narrow-bound kernel when its blocks stay
+    // resident with one block per SM
+    bool narrow = false;
+    if (block_team && threads <= kNarrowThreads) {
+        int per_sm = 0;
+        if (engine_max_blocks_per_sm(false, true, true, threads, plan.total, &per_sm) == cudaSuccess &&
+            (int64_t)per_sm * sms >= group)
+            narrow = true;
+    }
+    cfg.narrow = narrow;
     D.rpc = rpc;
     D.group = group;
     D.teams = teams;
@@ -335,7 +344,7 @@ int choose_config(const HostProblem& P, const pticm_opts& o, bool replay, Instan
     cfg.plan = plan;
     if (group > 1) {
         int per_sm = 0;
-        e = engine_max_blocks_per_sm(replay, block_team, threads, plan.total, &per_sm);
+        e = engine_max_blocks_per_sm(replay, block_team, narrow, threads, plan.total, &per_sm);
         if (e != cudaSuccess) { msg = cudaGetErrorString(e); return PTICM_ERR_CUDA; }
         if ((int64_t)per_sm * sms < group) {
             msg = "the replica blocks of one instance cannot all be resident (" + std::to_string(group) +
@@ -425,6 +434,7 @@ int configure(pticm_ctx* c, bool replay) {
     c->threads = cfg.threads;
     c->teams = cfg.teams;
     c->block_team = cfg.block_team;
+    c->narrow = cfg.narrow;
     c->plan = cfg.plan;
     finish_desc(c->desc, c->P, c->o, cfg);
     if (cfg.state_global || cfg.field_gather) {
@@ -945,7 +955,7 @@ int pticm_run(pticm_ctx* c, uint64_t pt_steps, uint32_t phase_mask) {
         A.nsteps = chunk;
         A.phase_mask = (int)phase_mask;
         CK(cudaEventRecord(c->ev0, c->stream));
-        CK(launch_engine(A, c->threads, false, c->block_team, c->group > 1, c->stream));
+        CK(launch_engine(A, c->threads, false, c->block_team, c->narrow, c->group > 1, c->stream));
         CK(cudaEventRecord(c->ev1, c->stream));
         CK(cudaEventSynchronize(c->ev1));
         float ms = 0.f;
@@ -1002,7 +1012,7 @@ int pticm_replay(pticm_ctx* c, const pticm_trace* t) {
     A.replay.n_xchg = xs.size();
     A.replay.n_icm = seeds.size();
     CK(cudaEventRecord(c->ev0, c->stream));
-    CK(launch_engine(A, c->threads, true, false, false, c->stream));
+    CK(launch_engine(A, c->threads, true, false, false, false, c->stream));
     CK(cudaEventRecord(c->ev1, c->stream));
     CK(cudaEventSynchronize(c->ev1));
     float ms = 0.f;

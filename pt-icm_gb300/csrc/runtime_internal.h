@@ -55,6 +55,7 @@ inline int32_t pad16(int64_t n) { return (int32_t)((n + 15) & ~15ll); }
 struct LaunchConfig {
     int rpc = 0, group = 0, threads = 0, teams = 1;
     bool block_team = false;
+    bool narrow = false;         // block team on the narrow-bound kernel (kNarrowThreads, 120 registers)
     bool state_global = false;   // replica state and ICM scratch in device memory
     bool field_gather = false;   // spins in shared memory, fields gathered at each visit
     SmemPlan plan{};
@@ -115,9 +116,9 @@ long long energy_bound(const HostProblem& P);
 const HostProblem& problem_host(const pticm_problem* p);
 void set_last_error(const std::string& m);
 
-cudaError_t launch_engine(const EngineArgs& A, int threads, bool replay, bool block_team, bool cooperative,
-                          cudaStream_t stream);
-cudaError_t engine_max_blocks_per_sm(bool replay, bool block_team, int threads, size_t smem, int* out);
+cudaError_t launch_engine(const EngineArgs& A, int threads, bool replay, bool block_team, bool narrow,
+                          bool cooperative, cudaStream_t stream);
+cudaError_t engine_max_blocks_per_sm(bool replay, bool block_team, bool narrow, int threads, size_t smem, int* out);
 cudaError_t launch_init_spins(const EngineArgs& A, const int32_t* rep_inst, int total_reps,
                               unsigned long long seed, cudaStream_t stream);
 cudaError_t launch_recompute(const EngineArgs& A, const int32_t* rep_inst, int total_reps, int write_back,

@@ -425,8 +425,8 @@ int pticm_batch_create(const pticm_problem* const* problems, uint32_t count, con
     if (o->chains < 1 || o->chains > 16) return bfail(PTICM_ERR_INVALID, "chains must be in [1, 16]");
     if (o->icm && (o->chains % 2)) return bfail(PTICM_ERR_INVALID, "ICM pairs chains: use an even chain count");
     if (o->sweeps < 1 || o->exchange > 1 || o->icm_algo > 3) return bfail(PTICM_ERR_INVALID, "invalid options");
-    if (o->block_threads && (o->block_threads % 32 || o->block_threads > 1024))
-        return bfail(PTICM_ERR_INVALID, "block_threads must be a multiple of 32, at most 1024");
+    if (o->block_threads && (o->block_threads % 32 || o->block_threads > (uint32_t)kNarrowThreads))
+        return bfail(PTICM_ERR_INVALID, "block_threads must be a multiple of 32, at most 512");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         return bfail(PTICM_ERR_NODEVICE, "no CUDA device is available; the PT-ICM engine has no CPU path");
@@ -438,7 +438,7 @@ int pticm_batch_create(const pticm_problem* const* problems, uint32_t count, con
     b->nt = (int)o->nt;
     b->C = (int)o->chains;
     b->R = b->nt * b->C;
-    b->threads = o->block_threads ? (int)o->block_threads : 1024;
+    b->threads = o->block_threads ? (int)o->block_threads : kNarrowThreads;
     b->P.reserve(count);
     for (uint32_t i = 0; i < count; i++) b->P.push_back(problem_host(problems[i]));
     // pools

@@ -1009,10 +1009,13 @@ __device__ void exchange_replay(const EngineArgs& A, const BlockCtx& B, int ls, 
 }
 
 // ---------------------------------------------------------------- kernel
-// NARROW: a block team of at most kNarrowThreads threads, one block per SM;
-// the bound leaves each thread 120 registers instead of 64.
+// Launch bounds: blocks of several replicas, and narrow block teams (NARROW),
+// run at most kNarrowThreads threads, which leaves each thread 120 registers
+// instead of the 64 of a 1024-thread bound; replay and wide block teams (one
+// replica of a large instance per block) keep 1024.
 template <bool REPLAY, bool BLOCKTEAM, bool NARROW>
-__global__ void __launch_bounds__(NARROW ? kNarrowThreads : 1024, 1) pt_engine_kernel(const EngineArgs A) {
+__global__ void __launch_bounds__((REPLAY || (BLOCKTEAM && !NARROW)) ? 1024 : kNarrowThreads, 1)
+    pt_engine_kernel(const EngineArgs A) {
     extern __shared__ __align__(128) uint8_t smem[];
     // the job's context and the profiling counters: one copy per block (per-
     // thread copies of uniform values would live in local memory)
@@ -1485,7 +1488,7 @@ cudaError_t launch_engine(const EngineArgs& A, int threads, bool replay, bool bl
 }
 
 cudaError_t engine_max_blocks_per_sm(bool replay, bool block_team, bool narrow, int threads, size_t smem, int* out) {
-    if (narrow && threads > kNarrowThreads) {
+    if (!replay && (narrow || !block_team) && threads > kNarrowThreads) {
         *out = 0;
         return cudaSuccess;
     }

@@ -166,8 +166,8 @@ enum EngineFlags : int32_t {
 
 // Shared-memory scratch of one ICM team for an instance of n_pad sites: BFS
 // queue / labels (4 B per site), overlap flags (1 B per site), visited bits.
-// Threads of a block-team block launched with the narrow bound (one block
-// per SM, 120 registers a thread).
+// Threads of a block of several replicas, or of a block team launched with
+// the narrow bound (120 registers a thread).
 constexpr int kNarrowThreads = 512;
 
 inline constexpr uint32_t icm_team_bytes(int32_t n_pad) {

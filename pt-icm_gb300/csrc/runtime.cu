@@ -233,13 +233,18 @@ int choose_config(const HostProblem& P, const pticm_opts& o, bool replay, Instan
     int threads = (int)o.block_threads;
     if (replay) threads = std::min(1024, 32 * std::max(1, std::min(R, 32)));
     if (threads <= 0) {
-        if (rpc > 1) threads = 1024;
-        // one replica per block: at most the narrow-bound block (on N=2000,
-        // 512 threads at 120 registers beat 1024 threads at 64 by 11 %)
+        // several replicas per block: the 512-thread bound; one replica per
+        // block: at most the narrow-bound block (on N=2000, 512 threads at
+        // 120 registers beat 1024 threads at 64 by 11 %)
+        if (rpc > 1) threads = kNarrowThreads;
         else threads = std::min(kNarrowThreads, std::max(128, ((std::max(max_class, n / 2) + 31) / 32) * 32));
     }
     if (threads % 32 != 0 || threads > 1024) {
         msg = "block_threads must be a multiple of 32, at most 1024";
+        return PTICM_ERR_INVALID;
+    }
+    if (!replay && rpc > 1 && threads > kNarrowThreads) {
+        msg = "block_threads must be at most 512 with several replicas per block";
         return PTICM_ERR_INVALID;
     }
     bool block_team = (rpc == 1) && !replay;

@@ -4,16 +4,18 @@
 //   C[M x N] = act(A[M x K] . B[N x K]^T + bias[N])      (A, B bf16, K-major)
 //
 // One CTA of 128 threads computes a 128 x BN tile (BN = 128, or 256 when
-// N > 128).  K advances in chunks of 64 through two shared-memory staging
+// N > 128).  K advances in chunks of 64 through TC_STAGES shared-memory
 // buffers in the canonical K-major layout without swizzle: 8-row x 16-byte
 // core matrices, K-adjacent core matrices 128 B apart (leading byte offset),
-// 8-row groups 1024 B apart (stride byte offset).  Thread 0 issues
-// tcgen05.mma.kind::f16 (M=128, N=BN, K=16 each, FP32 accumulation) into a
-// tensor-memory accumulator and commits each chunk to its buffer's mbarrier;
-// the threads stage the next chunk meanwhile.  The four warps then read
-// their 32 accumulator lanes with tcgen05.ld and apply the epilogue (bias,
-// optional SiLU, FP32 and/or BF16 stores).  Every wait is bounded; a timeout
-// is recorded in a status word.
+// 8-row groups 1024 B apart (stride byte offset).  The threads fill the
+// buffers with 16-byte cp.async copies, TC_STAGES - 1 chunks ahead of the
+// tensor cores.  Thread 0 issues tcgen05.mma.kind::f16 (M=128, N=BN, K=16
+// each, FP32 accumulation) into a tensor-memory accumulator and commits each
+// chunk to its buffer's mbarrier, which the threads wait on before they
+// refill that buffer.  The four warps then read their 32 accumulator lanes
+// with tcgen05.ld and apply the epilogue (bias, optional SiLU, FP32 and/or
+// BF16 stores, 16 bytes at a time when aligned).  Every wait is bounded; a
+// timeout is recorded in a status word.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -49,33 +51,37 @@ __device__ __forceinline__ void tc_fence_proxy_async() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-// Copy a tile of `nrows` x 64 bf16 (rows r0.., columns k0..) of a K-major
-// matrix into the core-matrix layout (8-row x 16-byte core matrices, K-
-// adjacent ones 128 B apart, 8-row groups 1024 B apart); thread t moves rows
-// t, t+128, ...; rows past `rows` are zero.
-__device__ __forceinline__ void tc_stage_tile(uint8_t* dst, const __nv_bfloat16* src, long long ld, int r0, int k0,
-                                              int rows, int nrows) {
-    for (int m = threadIdx.x; m < nrows; m += blockDim.x) {
-        uint4 v[8];
-        if (r0 + m < rows) {
-            const uint4* p = reinterpret_cast<const uint4*>(src + (long long)(r0 + m) * ld + k0);
-#pragma unroll
-            for (int c = 0; c < 8; c++) v[c] = __ldg(p + c);
-        } else {
-#pragma unroll
-            for (int c = 0; c < 8; c++) v[c] = make_uint4(0, 0, 0, 0);
-        }
-        uint8_t* base = dst + (m >> 3) * 1024 + (m & 7) * 16;
-#pragma unroll
-        for (int c = 0; c < 8; c++) *reinterpret_cast<uint4*>(base + c * 128) = v[c];
+constexpr int TC_STAGES = 4;
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Issue the copies of a tile of `nrows` x 64 bf16 (rows r0.., columns k0..)
+// of a K-major matrix into the core-matrix layout (8-row x 16-byte core
+// matrices, K-adjacent ones 128 B apart, 8-row groups 1024 B apart).  Lane
+// pairs of 16-byte pieces cover a row's 128 bytes; rows past `rows` are
+// zero-filled (no bytes read).
+__device__ __forceinline__ void tc_stage_tile_async(uint8_t* dst, const __nv_bfloat16* src, long long ld, int r0,
+                                                    int k0, int rows, int nrows) {
+    const uint32_t d0 = smem_u32(dst);
+    for (int idx = threadIdx.x; idx < nrows * 8; idx += blockDim.x) {
+        const int m = idx >> 3, c = idx & 7;
+        const bool in = r0 + m < rows;
+        const __nv_bfloat16* p = in ? src + (long long)(r0 + m) * ld + k0 + c * 8 : src;
+        cp_async16(d0 + (uint32_t)((m >> 3) * 1024 + (m & 7) * 16 + c * 128), p, in ? 16u : 0u);
     }
 }
 
-// One CTA computes a 128 x BN tile.  K advances in chunks of 64 through two
-// staging buffers: while the tensor cores run chunk k (issued by thread 0,
-// committed to that buffer's mbarrier), the threads stage chunk k+1 into
-// the other buffer, which they reuse only after the commit of chunk k-1 has
-// arrived.  Each mbarrier thus has at most one phase outstanding.
+// One CTA computes a 128 x BN tile.  Chunk kc lives in buffer kc % TC_STAGES;
+// after the MMAs of chunk kc are issued, the buffer of chunk kc - 1 is
+// refilled with chunk kc + TC_STAGES - 1 once the commit of chunk kc - 1 has
+// arrived (each mbarrier has at most one phase outstanding).  One cp.async
+// group is committed per iteration, so waiting until TC_STAGES - 2 groups
+// are pending means chunk kc + 1 has landed.
 template <int BN>
 __global__ void __launch_bounds__(128, 1)
 tc_gemm_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restrict__ B, int M, int N, int K,
@@ -84,7 +90,7 @@ tc_gemm_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restr
     constexpr uint32_t A_BYTES = TC_BM * TC_BK * 2;
     constexpr uint32_t STAGE = A_BYTES + BN * TC_BK * 2;
     extern __shared__ __align__(1024) uint8_t tc_smem[];
-    __shared__ uint64_t mbar[2];
+    __shared__ uint64_t mbar[TC_STAGES];
     __shared__ uint32_t tmem_base_s;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.x * TC_BM, n0 = blockIdx.y * BN;
@@ -96,25 +102,33 @@ tc_gemm_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restr
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    if (threadIdx.x == 0) {
-        mbar_init(&mbar[0], 1);
-        mbar_init(&mbar[1], 1);
-    }
+    if (threadIdx.x == 0)
+        for (int b = 0; b < TC_STAGES; b++) mbar_init(&mbar[b], 1);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base_s;
     const uint32_t idesc = tc_idesc_bf16(TC_BM, BN);
     const int nk = K / TC_BK;
-    uint32_t ph[2] = {0u, 0u};
+    uint32_t ph[TC_STAGES];
+    for (int b = 0; b < TC_STAGES; b++) ph[b] = 0u;
 
-    tc_stage_tile(buf0, A, K, m0, 0, M, TC_BM);
-    tc_stage_tile(buf0 + A_BYTES, B, K, n0, 0, N, BN);
-    tc_fence_proxy_async();
-    __syncthreads();
+    // prologue: chunks 0 .. TC_STAGES-2, one group each (empty past nk)
+    for (int c = 0; c < TC_STAGES - 1; c++) {
+        if (c < nk) {
+            uint8_t* dst = buf0 + c * STAGE;
+            tc_stage_tile_async(dst, A, K, m0, c * TC_BK, M, TC_BM);
+            tc_stage_tile_async(dst + A_BYTES, B, K, n0, c * TC_BK, N, BN);
+        }
+        cp_async_commit();
+    }
     bool ok = true;
     for (int kc = 0; kc < nk; kc++) {
-        const int b = kc & 1;
+        const int b = kc % TC_STAGES;
+        // chunk kc has landed: at most TC_STAGES-2 later groups are pending
+        cp_async_wait<TC_STAGES - 2>();
+        tc_fence_proxy_async();
+        __syncthreads();
         if (threadIdx.x == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t aaddr = smem_u32(buf0 + b * STAGE), baddr = aaddr + A_BYTES;
@@ -134,44 +148,45 @@ tc_gemm_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restr
                              smem_u32(&mbar[b]))
                          : "memory");
         }
-        if (kc + 1 < nk) {
-            const int nb = b ^ 1;
-            bool w = true;
-            if (kc >= 1) {   // the other buffer was read by the MMAs of chunk kc-1
-                w = mbar_wait_bounded(&mbar[nb], ph[nb]);
-                ph[nb] ^= 1u;
+        // refill the buffer of chunk kc-1 with chunk kc+TC_STAGES-1
+        const int nc = kc + TC_STAGES - 1;
+        bool w = true;
+        if (nc < nk) {
+            const int rb = nc % TC_STAGES;
+            if (kc >= 1) {   // that buffer was read by the MMAs of chunk kc-1
+                w = mbar_wait_bounded(&mbar[rb], ph[rb]);
+                ph[rb] ^= 1u;
             }
             if (w) {
-                uint8_t* dst = buf0 + nb * STAGE;
-                tc_stage_tile(dst, A, K, m0, (kc + 1) * TC_BK, M, TC_BM);
-                tc_stage_tile(dst + A_BYTES, B, K, n0, (kc + 1) * TC_BK, N, BN);
+                uint8_t* dst = buf0 + rb * STAGE;
+                tc_stage_tile_async(dst, A, K, m0, nc * TC_BK, M, TC_BM);
+                tc_stage_tile_async(dst + A_BYTES, B, K, n0, nc * TC_BK, N, BN);
             }
-            tc_fence_proxy_async();
-            ok = __syncthreads_and(w) != 0;
-            if (!ok) break;
         }
+        cp_async_commit();
+        ok = __syncthreads_and(w) != 0;
+        if (!ok) break;
     }
-    // drain: the commits of the last two chunks not yet waited for
+    cp_async_wait<0>();
+    // drain: the last commit arrives when every MMA issued before it is done
     if (ok) {
-        if (nk >= 2) {
-            const int b2 = (nk - 2) & 1;
-            ok = mbar_wait_bounded(&mbar[b2], ph[b2]);
-            ph[b2] ^= 1u;
-        }
-        const int b1 = (nk - 1) & 1;
-        ok = mbar_wait_bounded(&mbar[b1], ph[b1]) && ok;
+        const int bl = (nk - 1) % TC_STAGES;
+        ok = mbar_wait_bounded(&mbar[bl], ph[bl]);
     }
     ok = __syncthreads_and(ok) != 0;
     if (!ok) {
         // record the failure; give the MMAs in flight one more bounded wait
         // before the accumulator is released
         if (threadIdx.x == 0 && status) dev_fail(status, abort_flag, DEV_TMA_TIMEOUT, 100, blockIdx.x, blockIdx.y);
-        mbar_wait_bounded(&mbar[(nk - 1) & 1], ph[(nk - 1) & 1]);
+        mbar_wait_bounded(&mbar[(nk - 1) % TC_STAGES], ph[(nk - 1) % TC_STAGES]);
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
-    // epilogue: warp w owns accumulator lanes (rows) 32w .. 32w+31
+    // epilogue: warp w owns accumulator lanes (rows) 32w .. 32w+31; a row's
+    // 32 columns go out as 16-byte stores when the output rows are aligned
     const int row = m0 + warp * 32 + lane;
+    const bool vec_f = Cf == nullptr || (((reinterpret_cast<uintptr_t>(Cf) & 15) == 0) && (ldc & 3) == 0);
+    const bool vec_b = Cb == nullptr || (((reinterpret_cast<uintptr_t>(Cb) & 15) == 0) && (ldc & 7) == 0);
     if (ok) {
 #pragma unroll 1
         for (int c0 = 0; c0 < BN; c0 += 32) {
@@ -187,10 +202,37 @@ tc_gemm_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restr
                   "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
                 : "r"(taddr));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (row < M) {
+            if (row >= M) continue;
+            const int cb = n0 + c0;
+            if (cb + 32 <= N && vec_f && vec_b) {
+                float v[32];
+#pragma unroll
+                for (int j = 0; j < 32; j++) v[j] = __uint_as_float(r[j]) + (bias ? __ldg(bias + cb + j) : 0.0f);
+                if (Cf) {
+                    float4* o = reinterpret_cast<float4*>(Cf + (long long)row * ldc + cb);
+#pragma unroll
+                    for (int q = 0; q < 8; q++) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                }
+                if (act == TC_ACT_SILU)
+#pragma unroll
+                    for (int j = 0; j < 32; j++) v[j] = v[j] / (1.0f + __expf(-v[j]));
+                if (Cb) {
+                    uint4* o = reinterpret_cast<uint4*>(Cb + (long long)row * ldc + cb);
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        uint32_t w4[4];
+#pragma unroll
+                        for (int h = 0; h < 4; h++) {
+                            const __nv_bfloat162 t = __floats2bfloat162_rn(v[8 * q + 2 * h], v[8 * q + 2 * h + 1]);
+                            w4[h] = *reinterpret_cast<const uint32_t*>(&t);
+                        }
+                        o[q] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+                    }
+                }
+            } else {
 #pragma unroll
                 for (int j = 0; j < 32; j++) {
-                    const int col = n0 + c0 + j;
+                    const int col = cb + j;
                     if (col >= N) continue;
                     float v = __uint_as_float(r[j]) + (bias ? bias[col] : 0.0f);
                     if (Cf) Cf[(long long)row * ldc + col] = v;
@@ -212,15 +254,18 @@ tc_gemm_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restr
 cudaError_t tc_gemm(const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N, int K, const float* bias, int act,
                     float* Cf, __nv_bfloat16* Cb, long long ldc, DevStatus* status, int* abort_flag,
                     cudaStream_t st) {
+    if (M <= 0 || N <= 0 || K < TC_BK || K % TC_BK != 0 ||
+        ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) & 15))
+        return cudaErrorInvalidValue;
     if (N > 128) {
-        const size_t smem = 2 * (size_t)(TC_BM * TC_BK * 2 + 256 * TC_BK * 2) + 1024;
+        const size_t smem = TC_STAGES * (size_t)(TC_BM * TC_BK * 2 + 256 * TC_BK * 2) + 1024;
         cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         dim3 grid((M + TC_BM - 1) / TC_BM, (N + 255) / 256);
         tc_gemm_kernel<256><<<grid, 128, smem, st>>>(A, B, M, N, K, bias, act, Cf, Cb, ldc, status, abort_flag);
         return cudaGetLastError();
     }
-    const size_t smem = 2 * (size_t)(TC_BM * TC_BK * 2 + 128 * TC_BK * 2) + 1024;
+    const size_t smem = TC_STAGES * (size_t)(TC_BM * TC_BK * 2 + 128 * TC_BK * 2) + 1024;
     cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid((M + TC_BM - 1) / TC_BM, (N + 127) / 128);

@@ -4,8 +4,8 @@
 //   C[M x N] = act(A[M x K] . B[N x K]^T + bias[N])      (A, B bf16, K-major)
 //
 // One CTA of 128 threads computes a 128 x BN tile (BN = 128, or 256 when
-// N > 128).  K advances in chunks of 64 through TC_STAGES shared-memory
-// buffers in the canonical K-major layout without swizzle: 8-row x 16-byte
+// N > 128).  K advances in chunks of 64 through TC_STAGES (2 or 3) shared-
+// memory buffers in the canonical K-major layout without swizzle: 8-row x 16-byte
 // core matrices, K-adjacent core matrices 128 B apart (leading byte offset),
 // 8-row groups 1024 B apart (stride byte offset).  The threads fill the
 // buffers with 16-byte cp.async copies, TC_STAGES - 1 chunks ahead of the
@@ -51,7 +51,6 @@ __device__ __forceinline__ void tc_fence_proxy_async() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-constexpr int TC_STAGES = 4;
 
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, uint32_t src_bytes) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
@@ -82,7 +81,7 @@ __device__ __forceinline__ void tc_stage_tile_async(uint8_t* dst, const __nv_bfl
 // arrived (each mbarrier has at most one phase outstanding).  One cp.async
 // group is committed per iteration, so waiting until TC_STAGES - 2 groups
 // are pending means chunk kc + 1 has landed.
-template <int BN>
+template <int BN, int TC_STAGES>
 __global__ void __launch_bounds__(128, 1)
 tc_gemm_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restrict__ B, int M, int N, int K,
                const float* __restrict__ bias, int act, float* __restrict__ Cf, __nv_bfloat16* __restrict__ Cb,
@@ -248,6 +247,19 @@ tc_gemm_kernel(const __nv_bfloat16* __restrict__ A, const __nv_bfloat16* __restr
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
 }
 
+template <int BN, int STAGES>
+static cudaError_t tc_launch(const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N, int K, const float* bias,
+                             int act, float* Cf, __nv_bfloat16* Cb, long long ldc, DevStatus* status,
+                             int* abort_flag, cudaStream_t st) {
+    const size_t smem = STAGES * (size_t)(TC_BM * TC_BK * 2 + BN * TC_BK * 2) + 1024;
+    cudaError_t e =
+        cudaFuncSetAttribute(tc_gemm_kernel<BN, STAGES>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((M + TC_BM - 1) / TC_BM, (N + BN - 1) / BN);
+    tc_gemm_kernel<BN, STAGES><<<grid, 128, smem, st>>>(A, B, M, N, K, bias, act, Cf, Cb, ldc, status, abort_flag);
+    return cudaGetLastError();
+}
+
 // Launch: M, N multiples of 128 not required (rows/cols beyond are masked),
 // K a multiple of 64 and both operands 16-byte aligned with row stride K.
 // N > 128 uses 128 x 256 tiles (one CTA covers a 256-wide layer).
@@ -257,20 +269,11 @@ cudaError_t tc_gemm(const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N
     if (M <= 0 || N <= 0 || K < TC_BK || K % TC_BK != 0 ||
         ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) & 15))
         return cudaErrorInvalidValue;
-    if (N > 128) {
-        const size_t smem = TC_STAGES * (size_t)(TC_BM * TC_BK * 2 + 256 * TC_BK * 2) + 1024;
-        cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        dim3 grid((M + TC_BM - 1) / TC_BM, (N + 255) / 256);
-        tc_gemm_kernel<256><<<grid, 128, smem, st>>>(A, B, M, N, K, bias, act, Cf, Cb, ldc, status, abort_flag);
-        return cudaGetLastError();
-    }
-    const size_t smem = TC_STAGES * (size_t)(TC_BM * TC_BK * 2 + 128 * TC_BK * 2) + 1024;
-    cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    dim3 grid((M + TC_BM - 1) / TC_BM, (N + 127) / 128);
-    tc_gemm_kernel<128><<<grid, 128, smem, st>>>(A, B, M, N, K, bias, act, Cf, Cb, ldc, status, abort_flag);
-    return cudaGetLastError();
+    // stage counts that leave room for two CTAs per SM (97 KB each): one
+    // CTA's epilogue overlaps the other's loads (8192^3: 366 TFLOP/s against
+    // 331 with four stages and one CTA)
+    if (N > 128) return tc_launch<256, 2>(A, B, M, N, K, bias, act, Cf, Cb, ldc, status, abort_flag, st);
+    return tc_launch<128, 3>(A, B, M, N, K, bias, act, Cf, Cb, ldc, status, abort_flag, st);
 }
 
 }  // namespace pticm

@@ -325,14 +325,37 @@ static int32_t colour_graph(const HostProblem& P, std::vector<int32_t>& colour) 
     if (nc > 2 && nc <= 64) {
         std::vector<uint64_t> used(n, 0);
         std::vector<int32_t> sat(n, 0), dc(n, -1);
-        std::set<std::tuple<int32_t, int64_t, int64_t>> pq;   // (-sat, -deg, v)
-        for (int64_t v = 0; v < n; v++) pq.insert({0, -(P.row[v + 1] - P.row[v]), v});
+        // priority (saturation, degree, -index): vertices are ranked once by
+        // (degree desc, index asc), and each saturation level keeps a bitmap
+        // over ranks, so the next vertex is the lowest rank of the highest
+        // non-empty level (lo[] bounds the first non-zero word of a level)
+        std::vector<int64_t> ord(n), rank(n);
+        for (int64_t i = 0; i < n; i++) ord[i] = i;
+        std::stable_sort(ord.begin(), ord.end(), [&](int64_t x, int64_t y) {
+            return (P.row[x + 1] - P.row[x]) > (P.row[y + 1] - P.row[y]);
+        });
+        for (int64_t r = 0; r < n; r++) rank[ord[r]] = r;
+        const int64_t W = (n + 63) / 64;
+        const int levels = nc + 1;
+        std::vector<uint64_t> bits((size_t)levels * (size_t)W, 0);
+        std::vector<int64_t> cnt(levels, 0), lo(levels, W);
+        for (int64_t r = 0; r < n; r++) bits[(size_t)(r >> 6)] |= 1ull << (r & 63);
+        cnt[0] = n;
+        lo[0] = 0;
+        int top = 0;
         int32_t nd = 0;
         bool fits = true;
-        while (!pq.empty() && fits) {
-            const auto top = *pq.begin();
-            pq.erase(pq.begin());
-            const int64_t u = std::get<2>(top);
+        for (int64_t done = 0; done < n && fits; done++) {
+            while (top > 0 && cnt[top] == 0) top--;
+            uint64_t* lv = bits.data() + (size_t)top * (size_t)W;
+            int64_t wi = lo[top];
+            while (wi < W && lv[wi] == 0) wi++;
+            if (wi == W) { fits = false; break; }   // (cannot happen: cnt[top] > 0)
+            lo[top] = wi;
+            const int64_t r0 = wi * 64 + __builtin_ctzll(lv[wi]);
+            lv[wi] &= ~(1ull << (r0 & 63));
+            cnt[top]--;
+            const int64_t u = ord[r0];
             int32_t c = 0;
             while (c < 64 && (used[u] >> c) & 1ull) c++;
             if (c >= nc) { fits = false; break; }   // no better than greedy
@@ -341,10 +364,17 @@ static int32_t colour_graph(const HostProblem& P, std::vector<int32_t>& colour) 
             for (int64_t a = P.row[u]; a < P.row[u + 1]; a++) {
                 const int64_t v = P.col[a];
                 if (dc[v] >= 0 || ((used[v] >> c) & 1ull)) continue;
-                pq.erase({-sat[v], -(P.row[v + 1] - P.row[v]), v});
                 used[v] |= 1ull << c;
-                sat[v]++;
-                pq.insert({-sat[v], -(P.row[v + 1] - P.row[v]), v});
+                const int sv = sat[v]++;
+                if (sv + 1 >= levels) { fits = false; break; }
+                const int64_t rv = rank[v], w = rv >> 6;
+                const uint64_t bit = 1ull << (rv & 63);
+                bits[(size_t)sv * (size_t)W + (size_t)w] &= ~bit;
+                cnt[sv]--;
+                bits[(size_t)(sv + 1) * (size_t)W + (size_t)w] |= bit;
+                cnt[sv + 1]++;
+                lo[sv + 1] = std::min(lo[sv + 1], w);
+                top = std::max(top, sv + 1);
             }
         }
         if (fits && nd < nc) {

@@ -1421,6 +1421,19 @@ __global__ void init_spins_kernel(const EngineArgs A, const int32_t* rep_inst, i
     }
 }
 
+// States given by the caller (R x n bytes, 0/1, original site order) into
+// the device order as +-1 spins: replica r's site i goes to iperm[i];
+// padding sites hold +1.
+__global__ void load_states_kernel(const uint8_t* src, const int32_t* iperm, int8_t* spins, int R, int n, int n_pad) {
+    const long long total = (long long)R * n_pad;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(idx / n_pad), i = (int)(idx - (long long)r * n_pad);
+        if (i < n) spins[(long long)r * n_pad + iperm[i]] = src[(long long)r * n + i] ? (int8_t)1 : (int8_t)-1;
+        else spins[idx] = 1;
+    }
+}
+
 // Philox outputs for host-side known-answer checks.
 __global__ void philox_probe_kernel(const uint4* ctr, const uint2* key, uint4* out, int count) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1508,6 +1521,14 @@ cudaError_t launch_recompute(const EngineArgs& A, const int32_t* rep_inst, int t
 cudaError_t launch_init_spins(const EngineArgs& A, const int32_t* rep_inst, int total_reps,
                               unsigned long long seed, cudaStream_t stream) {
     init_spins_kernel<<<total_reps, 256, 0, stream>>>(A, rep_inst, total_reps, seed);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_load_states(const uint8_t* src, const int32_t* iperm, int8_t* spins, int R, int n, int n_pad,
+                               cudaStream_t stream) {
+    const long long total = (long long)R * n_pad;
+    const int blocks = (int)std::min<long long>((total + 255) / 256, 4096);
+    load_states_kernel<<<blocks, 256, 0, stream>>>(src, iperm, spins, R, n, n_pad);
     return cudaGetLastError();
 }
 

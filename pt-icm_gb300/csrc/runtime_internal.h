@@ -119,6 +119,8 @@ void set_last_error(const std::string& m);
 cudaError_t launch_engine(const EngineArgs& A, int threads, bool replay, bool block_team, bool narrow,
                           bool cooperative, cudaStream_t stream);
 cudaError_t engine_max_blocks_per_sm(bool replay, bool block_team, bool narrow, int threads, size_t smem, int* out);
+cudaError_t launch_load_states(const uint8_t* src, const int32_t* iperm, int8_t* spins, int R, int n, int n_pad,
+                               cudaStream_t stream);
 cudaError_t launch_init_spins(const EngineArgs& A, const int32_t* rep_inst, int total_reps,
                               unsigned long long seed, cudaStream_t stream);
 cudaError_t launch_recompute(const EngineArgs& A, const int32_t* rep_inst, int total_reps, int write_back,

@@ -159,8 +159,9 @@ struct BlockCtx {
     int32_t* tb;        // threshold row base of each local replica
 };
 
-// ICM team scratch: BFS queue (n ints), overlap flags (n bytes), visited
-// bits; the layout matches icm_team_bytes of the shared-memory plan.
+// ICM team scratch: BFS queue / union-find parents (n ints), overlap flags
+// (n bytes), visited bits (icm_team_bytes); a block team's overlap list (n
+// ints) follows (icm_block_bytes of the shared-memory plan).
 struct IcmScratch {
     int* queue;
     uint8_t* d;
@@ -275,7 +276,8 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
             append(i2 < n, a2 != b2, i2);
         }
     }
-    for (int w = team.tr; w < nwords; w += team.ts) X.vis[w] = 0u;
+    if (algo == ENGINE_ICM_BFS)   // the visited bits of the breadth-first search
+        for (int w = team.tr; w < nwords; w += team.ts) X.vis[w] = 0u;
     team.reduce(cnt, kd, ke, hs);
     const bool gflip = cnt > (long long)(n / 2);
     // the overlap list of a block team: [l0, l0 + llen) of lst
@@ -1259,12 +1261,10 @@ __global__ void __launch_bounds__((REPLAY || (BLOCKTEAM && !NARROW)) ? 1024 : kN
         P.tick(PROF_EXCHANGE);
         if (icm_on) {
             // pairs q = cp*nc + kk: slots (2cp)*nt + k and (2cp+1)*nt + k, k = nt-1-kk
-            const int npairs = D.nc * (D.chains / 2);
             // the block's pairs, found from its own replicas' slots: replica
             // j at slot s (chain c = s / nt, temperature k = s % nt) is in pair
             // q = (c / 2) nc + (nt-1-k) when nt-1-k < nc; a pair with both
             // replicas in the block is taken from its first chain's side
-            (void)npairs;
             const int chains_even = D.chains & ~1;
             // the whole block is one team when it holds one replica, or when
             // the instance is configured with one team (large instances: a

@@ -50,10 +50,10 @@ def _graph():
     return instances.c2()
 
 
-def _profiled_traffic():
-    """DRAM bytes per engine launch from the committed ncu summary."""
+def _profiled_traffic(summary="pt_engine_c2_bench.md"):
+    """DRAM bytes per engine launch from a committed ncu summary."""
     try:
-        with open(os.path.join(ROOT, "profiles", "pt_engine_c2_bench.md")) as f:
+        with open(os.path.join(ROOT, "profiles", summary)) as f:
             for line in f:
                 if line.startswith("| traffic_bytes_per_launch |"):
                     return int(line.split("|")[2].strip())
@@ -435,6 +435,7 @@ LARGE_WORKLOAD = ("random +-1 MaxCut graph N=20000, mean degree 40 (M=400000, se
 
 
 def run_gpu_large(args):
+    import numpy as np
     import torch
     import pticm
     from pticm import instances as I
@@ -459,6 +460,38 @@ def run_gpu_large(args):
     total_ms = sum(dev_ms)
     sites = 512 * inst.n
     value = sites * steps_per * args.steps / (total_ms / 1000.0)
+    mism = ctx.verify()
+    # end to end from host buffers: the problem from its edge list, the
+    # ladder, the warmed-up replicas as initial states (each to the replica
+    # that starts at its temperature), 100 PT steps, best state and
+    # statistics back
+    beta = pticm.beta_linspace(0.5, 9.5, 128)
+    s_now, _, _, slot_now = ctx.replicas()
+    by_slot = np.empty_like(s_now)
+    by_slot[slot_now] = s_now
+    states_host = torch.from_numpy(by_slot).pin_memory()
+    src = np.ascontiguousarray(inst.src, np.int32)
+    dst = np.ascontiguousarray(inst.dst, np.int32)
+    w = np.ascontiguousarray(inst.w, np.float64)
+    e2e_pt = 100
+    h2d = src.nbytes + dst.nbytes + w.nbytes + beta.nbytes + states_host.numel()
+    d2h = 0
+    e2e_t = []
+    for i in range(args.e2e_steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        p2 = pticm.Problem.from_coo(inst.n, src, dst, w)
+        c2 = pticm.Context(p2, nt=128, chains=4, seed=100 + i, icm=True)
+        c2.set_ladder(beta)
+        c2.set_states(states_host.numpy())
+        c2.run(e2e_pt)
+        E, sweep, best, rep = c2.best()
+        st2, att, suc = c2.stats()
+        d2h = best.nbytes + 16 + att.nbytes + suc.nbytes + 64
+        del c2, p2
+        torch.cuda.synchronize()
+        if i > 0:
+            e2e_t.append(time.perf_counter() - t0)
     peak, peak_kind = _peaks()
     bytes_per_sweep = (2 * inst.n + 12 * inst.m) * 512
     achieved = bytes_per_sweep * steps_per / (total_ms / 1000.0 / args.steps) / 1e9
@@ -466,10 +499,17 @@ def run_gpu_large(args):
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int8 spins, int32 fields/energies",
             "data": "synthetic", "config": {"workload": LARGE_WORKLOAD, "ncolors": info.ncolors,
-                                            "icm_pairs": int(ctx.ladder()[2]), "verify_mismatches_after": ctx.verify()},
+                                            "icm_pairs": int(ctx.ladder()[2]), "verify_mismatches_after": mism,
+                                            "l2": "the working set (about 170 MB) exceeds L2"},
+            "e2e": {"value": sites * e2e_pt / statistics.median(e2e_t), "unit": "attempts/s",
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "what": f"problem from its edge list (colouring on the host) + ladder + the warmed-up replicas "
+                            f"from pinned host memory + {e2e_pt} PT steps + best state/statistics back, per step"},
             "gpu_launches": args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": None, "note": f"algorithmic bytes 2N+12M per replica-sweep; peak {peak_kind}"},
+                         "traffic": _profiled_traffic("pt_engine_large_c5.md"),
+                         "note": f"algorithmic bytes 2N+12M per replica-sweep; peak {peak_kind}; traffic = ncu DRAM "
+                                 "bytes per launch (profiles/pt_engine_large_c5.md)"},
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
     return 0

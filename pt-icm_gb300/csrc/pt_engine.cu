@@ -612,12 +612,24 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
 // mode, where fields are not stored): f_i = sum_j J_ij s_j.
 __device__ __forceinline__ int gather_field(const int32_t* row, const uint32_t* adj, const int8_t* sp, int i) {
     int f = 0;
+    int a = row[i];
     const int e1 = row[i + 1];
-#pragma unroll 4
-    for (int a = row[i]; a < e1; a++) {
-        const uint32_t e = adj[a];   // plain load: adj may be staged in shared memory
-        f += (int)(int8_t)(e & 0xffu) * sp[e >> 8];
+    auto term = [&](uint32_t e) { f += (int)(int8_t)(e & 0xffu) * sp[e >> 8]; };
+    // plain loads (adj may be staged in shared memory): a scalar head up to
+    // a 16-byte boundary, then four entries per load, then the tail
+    if ((reinterpret_cast<uintptr_t>(adj) & 15u) == 0) {
+        for (; a < e1 && (a & 3); a++) term(adj[a]);
+#pragma unroll 2
+        for (; a + 4 <= e1; a += 4) {
+            const uint4 q = *reinterpret_cast<const uint4*>(adj + a);
+            term(q.x);
+            term(q.y);
+            term(q.z);
+            term(q.w);
+        }
     }
+#pragma unroll 4
+    for (; a < e1; a++) term(adj[a]);
     return f;
 }
 

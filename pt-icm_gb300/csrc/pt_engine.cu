@@ -178,6 +178,31 @@ __device__ __forceinline__ IcmScratch icm_scratch(uint8_t* base, int n_pad) {
     return X;
 }
 
+// Calls f(e) for every packed entry (col << 8 | uint8 J) of site i's
+// neighbour list: a scalar head up to a 16-byte boundary, four entries per
+// 16-byte load, a scalar tail (plain loads: the list may be staged in shared
+// memory; a list that is not 16-byte aligned is walked entry by entry).
+// For small bodies only (field gathers and pushes): the body is expanded
+// several times, and a large one (union-find) costs more in instruction
+// fetch than the wider loads save.
+template <class F>
+__device__ __forceinline__ void for_each_neighbour(const int32_t* row, const uint32_t* adj, int i, F&& f) {
+    int a = row[i];
+    const int e1 = row[i + 1];
+    if ((reinterpret_cast<uintptr_t>(adj) & 15u) == 0) {
+        for (; a < e1 && (a & 3); a++) f(adj[a]);
+#pragma unroll 2
+        for (; a + 4 <= e1; a += 4) {
+            const uint4 q = *reinterpret_cast<const uint4*>(adj + a);
+            f(q.x);
+            f(q.y);
+            f(q.z);
+            f(q.w);
+        }
+    }
+    for (; a < e1; a++) f(adj[a]);
+}
+
 // ------------------------------------------------------------------ ICM
 // One cluster move on the pair (A, B) = (chain 2c, chain 2c+1) at slot k.
 // The team computes the overlap (sites where A and B differ), the
@@ -612,24 +637,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
 // mode, where fields are not stored): f_i = sum_j J_ij s_j.
 __device__ __forceinline__ int gather_field(const int32_t* row, const uint32_t* adj, const int8_t* sp, int i) {
     int f = 0;
-    int a = row[i];
-    const int e1 = row[i + 1];
-    auto term = [&](uint32_t e) { f += (int)(int8_t)(e & 0xffu) * sp[e >> 8]; };
-    // plain loads (adj may be staged in shared memory): a scalar head up to
-    // a 16-byte boundary, then four entries per load, then the tail
-    if ((reinterpret_cast<uintptr_t>(adj) & 15u) == 0) {
-        for (; a < e1 && (a & 3); a++) term(adj[a]);
-#pragma unroll 2
-        for (; a + 4 <= e1; a += 4) {
-            const uint4 q = *reinterpret_cast<const uint4*>(adj + a);
-            term(q.x);
-            term(q.y);
-            term(q.z);
-            term(q.w);
-        }
-    }
-#pragma unroll 4
-    for (; a < e1; a++) term(adj[a]);
+    for_each_neighbour(row, adj, i, [&](uint32_t e) { f += (int)(int8_t)(e & 0xffu) * sp[e >> 8]; });
     return f;
 }
 
@@ -680,12 +688,8 @@ __device__ void colored_sweep(const EngineArgs& A, const BlockCtx& B, unsigned l
                     acc_fl++;
                     if (fd) {
                         const int dl = -2 * s;
-                        const int e1 = row[i + 1];
-#pragma unroll 4
-                        for (int a = row[i]; a < e1; a++) {
-                            const uint32_t e = adj[a];
-                            atomicAdd(fd + (e >> 8), (int)(int8_t)(e & 0xffu) * dl);
-                        }
+                        for_each_neighbour(row, adj, i,
+                                           [&](uint32_t e) { atomicAdd(fd + (e >> 8), (int)(int8_t)(e & 0xffu) * dl); });
                     }
                 }
             }
@@ -712,11 +716,9 @@ __device__ void colored_sweep(const EngineArgs& A, const BlockCtx& B, unsigned l
                         sp[i] = (int8_t)-s;
                         if (fd) {
                             const int dl = -2 * s;
-                            const int e1 = row[i + 1];
-                            for (int a = row[i]; a < e1; a++) {
-                                const uint32_t e = adj[a];
+                            for_each_neighbour(row, adj, i, [&](uint32_t e) {
                                 atomicAdd(fd + (e >> 8), (int)(int8_t)(e & 0xffu) * dl);
-                            }
+                            });
                         }
                     }
                 }

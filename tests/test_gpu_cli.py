@@ -118,3 +118,30 @@ def test_cli_folder_csv(tmp_path):
         assert float(r["ene"]) == pytest.approx(prob.energy(state), abs=1e-9)
         assert float(r["cut"]) == pytest.approx(prob.maxcut(state), abs=1e-9)
         assert int(r["flips"]) > 0
+
+
+def test_cli_folder_preprocess_groups_by_ladder_length(tmp_path):
+    """With --preprocess every problem gets its own multihistogram ladder;
+    runs with ladders of different lengths go to different batches, and each
+    row reports its own ladder."""
+    import csv
+    import shutil
+    d = tmp_path / "problems"
+    d.mkdir()
+    names = ["pmL6.gset", "pmL10.gset", "rnd200_w1"]
+    for name in names:
+        shutil.copy(os.path.join(G, name), d / name)
+    out = tmp_path / "runs.csv"
+    _run("--folder", str(d), "--csv", str(out), "-s", "2", "-r", "12", "--pts", "200", "--icm",
+         "--preprocess", "--preprocess-samples", "300", "--sort-ladder")
+    with open(out) as f:
+        rows = list(csv.DictReader(f))
+    assert len(rows) == len(names)
+    for r in rows:
+        nt = int(r["replicas"])
+        tlist = [float(x) for x in r["tlist"][1:-1].split(";")]
+        assert 2 <= nt <= 12 and len(tlist) == 2 * nt
+        assert all(a <= b for a, b in zip(tlist[:nt], tlist[1:nt]))   # sorted ascending
+        prob = O.Problem.load(r["problem"], 0)
+        state = [int(c) for c in r["state"]]
+        assert float(r["ene"]) == pytest.approx(prob.energy(state), abs=1e-9)

@@ -441,12 +441,16 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                         }
                     });
                     team.sync();
-                    for_overlap([&](int u) {
-                        const int r = uf_find(vl, u);
-                        if (r < 0) ok = false;
-                        else vl[u] = r;
-                    });
-                    team.sync();
+                    if (round == 0) {
+                        // (after the last round the vote's and phase 3's
+                        // finds halve the paths they walk)
+                        for_overlap([&](int u) {
+                            const int r = uf_find(vl, u);
+                            if (r < 0) ok = false;
+                            else vl[u] = r;
+                        });
+                        team.sync();
+                    }
                 }
                 if (team.tr < 32) {
                     // vote over 32 sampled overlap sites (one warp): a block
@@ -456,7 +460,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                     // 16 bytes, bytes from n on are masked)
                     int cand = -1;
                     if (BLOCK) {
-                        cand = vl[lst[l0 + (int)(((long long)team.tr * llen) >> 5)]];
+                        cand = uf_find(vl, lst[l0 + (int)(((long long)team.tr * llen) >> 5)]);
                     } else {
                         const int w0 = (int)(((long long)team.tr * n) >> 7);
                         uint32_t fw[8];
@@ -466,7 +470,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                         for (int j = 0; j < 8 && cand < 0; j++)
                             for (int b = 0; b < 4; b++) {
                                 const int i = 4 * (w0 + j) + b;
-                                if (i < n && ((fw[j] >> (8 * b)) & 0xffu)) { cand = vl[i]; break; }
+                                if (i < n && ((fw[j] >> (8 * b)) & 0xffu)) { cand = uf_find(vl, i); break; }
                             }
                     }
                     const unsigned grp = __match_any_sync(0xffffffffu, cand);

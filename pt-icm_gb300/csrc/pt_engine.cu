@@ -355,6 +355,13 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
     if (threadIdx.x == 0) P.subtick(PROF_ICM_SEED);
     bool absolute = false;   // energies set from scratch (large flipped sets)
     int swapped = 0;         // the flipped set was D\C (the chains hold each other's result)
+    // a block team's union-find lists the sites it found outside the giant
+    // component L in the free part of lst (S, at sbase); when the flipped set
+    // lies in S it is taken from there: the sites of S whose final root is
+    // (fast_eq) or is not (!fast_eq) fast_root
+    bool fast = false, fast_eq = false;
+    int fast_root = -1, ns = 0;
+    const int sbase = l0 == 0 ? llen : 0;
     if (cnt > 0) {
         long long csize = 0;
         if (algo == ENGINE_ICM_BFS) {
@@ -486,6 +493,11 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                 const int L = *(volatile int*)team.ctl;
                 for_overlap([&](int u) {
                     if (uf_find(vl, u) == L) return;
+                    if (BLOCK) {
+                        // S never outgrows the free part of lst: |S| <= llen <= n - llen
+                        const int pos = atomicAdd(team.ctl + 4, 1);
+                        if (pos < llen) lst[sbase + pos] = u;
+                    }
                     const int e1 = B.row[u + 1];
 #pragma unroll 4
                     for (int a = B.row[u]; a < e1; a++) {
@@ -494,6 +506,25 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                     }
                 });
                 team.sync();
+                if (BLOCK) {
+                    // sites in L's component at their phase-3 check stay in it:
+                    // every site outside the final component of L is in S
+                    ns = min(*(volatile int*)(team.ctl + 4), llen);
+                    const int rL = uf_find(vl, L), rs = uf_find(vl, seed);
+                    long long c = 0;   // |S \ comp(L)| when the seed is in comp(L), else |C|
+                    for (int t = team.tr; t < ns; t += team.ts) {
+                        const int r = uf_find(vl, lst[sbase + t]);
+                        c += (rs == rL) ? (r != rL) : (r == rs);
+                    }
+                    unsigned long long m1 = ~0ull, m2 = ~0ull;
+                    long long none = 0;
+                    team.reduce(c, m1, m2, none);
+                    csize = (rs == rL) ? cnt - c : c;
+                    const bool sw = !REPLAY && csize * 2 > cnt;
+                    fast = (rs == rL) ? sw : !sw;   // the flipped set lies in S
+                    fast_root = rs == rL ? rL : rs;
+                    fast_eq = rs != rL;
+                }
             } else {
                 // minimum-label propagation with root hooking and pointer jumping
                 // (Shiloach-Vishkin style); labels only decrease and always name
@@ -537,14 +568,21 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
             if (!ok) dev_fail(A.status, A.abort_flag, DEV_UF_LIMIT, where_err + 3, q, algo);
             if (threadIdx.x == 0) P.subtick(PROF_ICM_UNION);
             const int root = (algo == ENGINE_ICM_UNION_FIND) ? uf_find(vl, seed) : vl[seed];
-            // mark the cluster C (d = 2) and count it
-            for_overlap([&](int u) {
-                const int lu = (algo == ENGINE_ICM_UNION_FIND) ? uf_find(vl, u) : vl[u];
-                if (lu != root) return;
-                d[u] = 2;
-                csize++;
-            });
-            {
+            if (BLOCK && algo == ENGINE_ICM_UNION_FIND) {
+                // csize is known; the general flip below needs C marked
+                if (!fast) {
+                    for_overlap([&](int u) {
+                        if (uf_find(vl, u) == root) d[u] = 2;
+                    });
+                }
+            } else {
+                // mark the cluster C (d = 2) and count it
+                for_overlap([&](int u) {
+                    const int lu = (algo == ENGINE_ICM_UNION_FIND) ? uf_find(vl, u) : vl[u];
+                    if (lu != root) return;
+                    d[u] = 2;
+                    csize++;
+                });
                 unsigned long long m1 = ~0ull, m2 = ~0ull;
                 long long none = 0;
                 team.reduce(csize, m1, m2, none);
@@ -560,7 +598,36 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
         swapped = (!REPLAY && csize * 2 > cnt) ? 1 : 0;
         const uint8_t fmark = swapped ? 1 : 2;
         const long long fsize = swapped ? cnt - csize : csize;
-        if (BLOCK && fsize * 4 > (long long)n) {
+        // one pass over a flipped site: flip it and push its field change to
+        // its neighbours; the energy changes by the edges leaving the flipped
+        // set F.  F is a union of overlap components, so a neighbour outside
+        // F is outside the overlap (equal in A and B) and keeps its spin.
+        auto flip_push = [&](int u) {
+            const int hu = D.has_h ? B.h[u] : 0;
+            int sa = 0, sb = 0;   // spins before the flip
+            if (locA) { sa = sA[u]; sA[u] = (int8_t)-sa; dEa -= 2 * sa * hu; }
+            if (locB) { sb = sB[u]; sB[u] = (int8_t)-sb; dEb -= 2 * sb * hu; }
+            const int e1 = B.row[u + 1];
+#pragma unroll 4
+            for (int a = B.row[u]; a < e1; a++) {
+                const uint32_t e = B.adj[a];
+                const int v = (int)(e >> 8);
+                const int J = (int)(int8_t)(e & 0xffu);
+                if (fA) atomicAdd(fA + v, J * (-2 * sa));
+                if (fB) atomicAdd(fB + v, J * (-2 * sb));
+                if (!d[v]) {
+                    const int sv = locA ? sA[v] : sB[v];
+                    if (locA) dEa -= 2 * J * sa * sv;
+                    if (locB) dEb -= 2 * J * sb * sv;
+                }
+            }
+        };
+        if (fast) {
+            for (int t = team.tr; t < ns; t += team.ts) {
+                const int u = lst[sbase + t];
+                if ((uf_find((volatile int*)X.queue, u) == fast_root) == fast_eq) flip_push(u);
+            }
+        } else if (BLOCK && fsize * 4 > (long long)n) {
             // a large cluster: flip, then fields and energies from scratch
             // (gathers, no atomics; the cost does not grow with the cluster)
             for_overlap([&](int u) {
@@ -592,31 +659,9 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
             }
             absolute = true;
         } else {
-            // a small cluster, flipped and pushed in one pass: each flipped
-            // site sends its field change to its neighbours, and the energy
-            // changes by the edges leaving the flipped set F.  F is a union
-            // of overlap components, so a neighbour outside F is outside the
-            // overlap (equal in A and B) and keeps its spin during the pass.
+            // a small flipped set, flipped and pushed in one pass
             for_overlap([&](int u) {
-                if (d[u] != fmark) return;
-                const int hu = D.has_h ? B.h[u] : 0;
-                int sa = 0, sb = 0;   // spins before the flip
-                if (locA) { sa = sA[u]; sA[u] = (int8_t)-sa; dEa -= 2 * sa * hu; }
-                if (locB) { sb = sB[u]; sB[u] = (int8_t)-sb; dEb -= 2 * sb * hu; }
-                const int e1 = B.row[u + 1];
-#pragma unroll 4
-                for (int a = B.row[u]; a < e1; a++) {
-                    const uint32_t e = B.adj[a];
-                    const int v = (int)(e >> 8);
-                    const int J = (int)(int8_t)(e & 0xffu);
-                    if (fA) atomicAdd(fA + v, J * (-2 * sa));
-                    if (fB) atomicAdd(fB + v, J * (-2 * sb));
-                    if (!d[v]) {
-                        const int sv = locA ? sA[v] : sB[v];
-                        if (locA) dEa -= 2 * J * sa * sv;
-                        if (locB) dEb -= 2 * J * sb * sv;
-                    }
-                }
+                if (d[u] == fmark) flip_push(u);
             });
         }
         team.sync();
@@ -631,6 +676,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
     if (BLOCK && team.tr == 0) {
         team.ctl[2] = 0;   // the list counters, for the next pair
         team.ctl[3] = 0;
+        team.ctl[4] = 0;
     }
     team.sync();
     if (threadIdx.x == 0) P.subtick(PROF_ICM_FLIP);
@@ -1170,8 +1216,9 @@ __global__ void __launch_bounds__((REPLAY || (BLOCKTEAM && !NARROW)) ? 1024 : kN
     if (tid == 0 && D.group > 1) bar_gen = *(volatile unsigned int*)(A.bar + 2 * inst + 1);
     if (tid == 0) {
         for (int q = 0; q < 3; q++) team_slot_reset(s_team_acc, q);
-        s_team_bc[2] = 0;   // the block team's overlap-list counters
+        s_team_bc[2] = 0;   // the block team's overlap-list and S counters
         s_team_bc[3] = 0;
+        s_team_bc[4] = 0;
     }
     __syncthreads();
     for (int k = tid; k + 1 < nt; k += T) s_dbeta[k] = s_beta[k] - s_beta[k + 1];

@@ -569,11 +569,15 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
             if (threadIdx.x == 0) P.subtick(PROF_ICM_UNION);
             const int root = (algo == ENGINE_ICM_UNION_FIND) ? uf_find(vl, seed) : vl[seed];
             if (BLOCK && algo == ENGINE_ICM_UNION_FIND) {
-                // csize is known; the general flip below needs C marked
+                // csize is known.  When the flipped set is not in S it is the
+                // rest of the overlap: mark the selected part of S (d = 3),
+                // and the flipped set is every overlap site not marked
                 if (!fast) {
-                    for_overlap([&](int u) {
-                        if (uf_find(vl, u) == root) d[u] = 2;
-                    });
+                    for (int t = team.tr; t < ns; t += team.ts) {
+                        const int u = lst[sbase + t];
+                        if ((uf_find(vl, u) == fast_root) == fast_eq) d[u] = 3;
+                    }
+                    team.sync();
                 }
             } else {
                 // mark the cluster C (d = 2) and count it
@@ -598,6 +602,9 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
         swapped = (!REPLAY && csize * 2 > cnt) ? 1 : 0;
         const uint8_t fmark = swapped ? 1 : 2;
         const long long fsize = swapped ? cnt - csize : csize;
+        // membership of an overlap site in the flipped set
+        const bool rest = BLOCK && algo == ENGINE_ICM_UNION_FIND && !fast;
+        auto in_flip = [&](int u) { return rest ? d[u] != 3 : d[u] == fmark; };
         // one pass over a flipped site: flip it and push its field change to
         // its neighbours; the energy changes by the edges leaving the flipped
         // set F.  F is a union of overlap components, so a neighbour outside
@@ -631,7 +638,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
             // a large cluster: flip, then fields and energies from scratch
             // (gathers, no atomics; the cost does not grow with the cluster)
             for_overlap([&](int u) {
-                if (d[u] != fmark) return;
+                if (!in_flip(u)) return;
                 if (locA) sA[u] = (int8_t)-sA[u];
                 if (locB) sB[u] = (int8_t)-sB[u];
             });
@@ -661,7 +668,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
         } else {
             // a small flipped set, flipped and pushed in one pass
             for_overlap([&](int u) {
-                if (d[u] == fmark) flip_push(u);
+                if (in_flip(u)) flip_push(u);
             });
         }
         team.sync();

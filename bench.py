@@ -664,7 +664,7 @@ def run_gpu_ladder(args):
                            "learned_accepted_mean": float(col("t_l")[col("fb") == 0].mean()) if (col("fb") == 0).any() else None,
                            "multihistogram_mean": float(col("t_m").mean())},
         "time_to_target": ttt,
-        "roofline": {"bound": "tensor", "kernel": "tc_gemm_kernel (tcgen05, BF16, FP32 accumulate)",
+        "roofline": {"bound": "tensor", "kernel": "tc_gemm_tma_kernel (TMA loads, tcgen05 MMA, BF16, FP32 accumulate)",
                      "achieved": gemm.get("65536x256x256", {}).get("tflops"), "peak": bf16_peak, "unit": "TFLOP/s",
                      "frac": (gemm.get("65536x256x256", {}).get("tflops") or 0.0) / bf16_peak,
                      "note": f"one 256x256 layer of the network on 65536 rows; peak {peak_kind} cuBLAS bf16",

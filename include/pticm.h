@@ -423,8 +423,10 @@ typedef struct pticm_learned_ladder_info {
  * exceeds tol (0.05), the ladder is placed again from the measured
  * acceptances (pticm_feedback_ladder) and checked again, at most three
  * times (not at all when the first check is off by more than 0.2); if it
- * still deviates, the multihistogram ladder of pticm_cae_ladder (2000
- * samples, 5000 burn-in) replaces it. */
+ * still deviates, a multihistogram ladder replaces it: from the energy
+ * histograms of the last check (two chains at its temperatures) when every
+ * pair of it accepted at least 5 % of its exchanges, else from the pilot
+ * run of pticm_cae_ladder (2000 samples, 5000 burn-in). */
 /* Feedback placement from measured acceptances acc[k] of the gaps of a
  * descending ladder: sigma_k = 2 erfc^-1(acc_k) / (beta_k - beta_{k+1}) (the
  * exchange acceptance of Gaussian energy distributions of width sigma is

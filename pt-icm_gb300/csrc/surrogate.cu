@@ -40,6 +40,7 @@ constexpr int kFeatures = 6;
 constexpr double kTargetScale = 10.0;
 constexpr int kChecks = 4;   // acceptance checks of a learned ladder: the surrogate's, then up to three feedback placements
 constexpr double kHopeless = 0.2;   // a first check this far off goes straight to the multihistogram ladder
+constexpr double kOverlapFloor = 0.05;   // lowest pair acceptance for which a check's histograms feed the fallback
 constexpr char kMagic[8] = {'P', 'T', 'I', 'C', 'M', 'M', 'L', 'P'};
 
 // ln N / 10, ln M / 12, mean degree / 20, degree std / 10, coupling mean and
@@ -249,9 +250,16 @@ int pticm_surrogate_ladder(const pticm_problem* p, pticm_mlp* m, double T0, doub
     return PTICM_OK;
 }
 
-int pticm_ladder_acceptance(const pticm_problem* p, const double* beta, uint32_t nt, uint64_t seed, uint64_t steps,
-                            uint64_t burn_in, double* acc) {
-    if (!p || !beta || !acc || nt < 2 || steps == 0) return sfail(PTICM_ERR_INVALID, "invalid arguments");
+}  // extern "C"
+
+namespace {
+
+// A PT run (two chains, no ICM) on a ladder: the exchange acceptance of each
+// neighbouring pair over `steps` steps after `burn_in`, and, when `hist` is
+// given, the per-slot energy histograms of those steps (R rows of nbins
+// bins, bin b at energy lo + 2b).
+int ladder_check(const pticm_problem* p, const double* beta, uint32_t nt, uint64_t seed, uint64_t steps,
+                 uint64_t burn_in, double* acc, std::vector<unsigned>* hist, int64_t* lo, uint64_t* nbins) {
     pticm_opts o;
     pticm_opts_default(&o);
     o.seed = seed;
@@ -263,6 +271,8 @@ int pticm_ladder_acceptance(const pticm_problem* p, const double* beta, uint32_t
     std::unique_ptr<pticm_ctx, void (*)(pticm_ctx*)> hold(c, pticm_destroy);
     if (int rc = pticm_set_ladder(c, beta, nt, 0)) return rc;
     if (int rc = pticm_init_states(c, seed)) return rc;
+    if (hist)
+        if (int rc = pticm_enable_energy_histograms(c, burn_in)) return rc;
     std::vector<uint64_t> a0(2 * nt), s0(2 * nt), a1(2 * nt), s1(2 * nt);
     if (burn_in)
         if (int rc = pticm_run(c, burn_in, PTICM_PHASE_SWEEP | PTICM_PHASE_EXCHANGE)) return rc;
@@ -274,7 +284,22 @@ int pticm_ladder_acceptance(const pticm_problem* p, const double* beta, uint32_t
         const double su = (double)(s1[k] - s0[k] + s1[k + nt] - s0[k + nt]);
         acc[k] = at > 0 ? su / at : 0.0;
     }
+    if (hist) {
+        if (int rc = pticm_get_energy_histograms(c, nullptr, lo, nbins)) return rc;
+        hist->assign((size_t)(2 * nt) * (size_t)*nbins, 0u);
+        if (int rc = pticm_get_energy_histograms(c, hist->data(), lo, nbins)) return rc;
+    }
     return PTICM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pticm_ladder_acceptance(const pticm_problem* p, const double* beta, uint32_t nt, uint64_t seed, uint64_t steps,
+                            uint64_t burn_in, double* acc) {
+    if (!p || !beta || !acc || nt < 2 || steps == 0) return sfail(PTICM_ERR_INVALID, "invalid arguments");
+    return ladder_check(p, beta, nt, seed, steps, burn_in, acc, nullptr, nullptr, nullptr);
 }
 
 int pticm_learned_ladder(const pticm_problem* p, pticm_mlp* m, double T0, double T1, int inverse, uint32_t nt,
@@ -290,11 +315,20 @@ int pticm_learned_ladder(const pticm_problem* p, pticm_mlp* m, double T0, double
     bool ok = cnt >= 2;
     double be = inverse ? T1 : 1 / T1, bs = inverse ? T0 : 1 / T0;
     if (bs < be) std::swap(bs, be);
+    // the energy histograms of the last check, and its ladder: the
+    // multihistogram fallback's samples
+    std::vector<unsigned> hist;
+    std::vector<double> hist_beta;
+    int64_t hist_lo = 0;
+    uint64_t hist_nbins = 0;
+    double hist_min_acc = 0.0;   // the lowest pair acceptance of that check
     for (int round = 0; ok && check_steps > 0 && round < kChecks; round++) {
         std::vector<double> acc(lad.size() - 1);
-        if (int rc = pticm_ladder_acceptance(p, lad.data(), (uint32_t)lad.size(), seed + round, check_steps,
-                                             check_steps / 4, acc.data()))
+        if (int rc = ladder_check(p, lad.data(), (uint32_t)lad.size(), seed + round, check_steps, check_steps / 4,
+                                  acc.data(), &hist, &hist_lo, &hist_nbins))
             return rc;
+        hist_beta = lad;
+        hist_min_acc = acc.empty() ? 0.0 : *std::min_element(acc.begin(), acc.end());
         double dev = 0;
         for (double a : acc) dev += std::fabs(a - r);
         li.mean_deviation = dev / (double)acc.size();
@@ -314,8 +348,22 @@ int pticm_learned_ladder(const pticm_problem* p, pticm_mlp* m, double T0, double
         *count = (uint32_t)lad.size();
     } else {
         li.fallback = 1;
-        if (int rc = pticm_cae_ladder(p, seed, T0, T1, inverse, nt, 2.0, 0.1, r, 2000, 5000, beta_out, count))
+        // the multihistogram ladder (src/cae_estimator.cc:155-428) from the
+        // samples the checks already drew: the last check's two chains at
+        // its temperatures, when every neighbouring pair of them exchanged
+        // often enough for their histograms to overlap; otherwise a
+        // separate pilot run (pticm_cae_ladder)
+        std::vector<double> dos, z;
+        double min_emin = 0;
+        uint64_t it = 0;
+        if (!hist.empty() && hist_min_acc >= kOverlapFloor &&
+            slot_hist_dos(hist.data(), (int)hist_beta.size(), 2, (long long)hist_nbins, (long long)hist_lo,
+                          hist_beta.data(), 2.0, dos, z, min_emin, it) == PTICM_OK) {
+            *count = cae_walk(dos, min_emin, 2.0, bs, be, 0.1, r, nt, beta_out);
+        } else if (int rc = pticm_cae_ladder(p, seed, T0, T1, inverse, nt, 2.0, 0.1, r, 2000, 5000, beta_out,
+                                             count)) {
             return rc;
+        }
     }
     if (info) *info = li;
     return PTICM_OK;

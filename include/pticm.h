@@ -370,7 +370,7 @@ PTICM_API int pticm_batch_logdos(pticm_batch* b, uint32_t inst, double estep, do
  * trained with Adam.  Parameters are one flat FP32 vector of
  * pticm_mlp_param_count() values: W1 [256 x 64] (input columns 7.. unused),
  * b1, W2 [256 x 256], b2, W3, b3, W4, b4, w5 [256], b5.  No counterpart in
- * the reference (the benchmark spec's learned ladder). */
+ * the reference: it serves the learned temperature ladder below. */
 typedef struct pticm_mlp pticm_mlp;
 PTICM_API int pticm_mlp_create(uint64_t seed, uint32_t batch, pticm_mlp** out);
 PTICM_API void pticm_mlp_destroy(pticm_mlp* m);

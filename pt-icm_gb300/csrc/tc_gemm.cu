@@ -5,7 +5,7 @@
 //
 // Two kernels compute the same 128 x BN tiles.  tc_gemm_tma_kernel (below)
 // brings the operands in with the tensor memory accelerator; the kernel here
-// is its fallback when the driver's tensor-map encoder is not available.
+// is its fallback when the CUDA driver's tensor-map encoder is not available.
 // One CTA of 128 threads computes a 128 x BN tile (BN = 128, or 256 when
 // N > 128).  K advances in chunks of 64 through TC_STAGES (2 or 3) shared-
 // memory buffers in the canonical K-major layout without swizzle: 8-row x 16-byte
@@ -433,7 +433,7 @@ static cudaError_t tc_launch(const __nv_bfloat16* A, const __nv_bfloat16* B, int
     return cudaGetLastError();
 }
 
-// The driver's tensor-map encoder, fetched once through the runtime (no
+// The CUDA driver's tensor-map encoder, fetched once through the runtime (no
 // link against the driver library).
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
@@ -487,7 +487,7 @@ cudaError_t tc_gemm(const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N
     if (M <= 0 || N <= 0 || K < TC_BK || K % TC_BK != 0 ||
         ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) & 15))
         return cudaErrorInvalidValue;
-    // operands through the tensor memory accelerator when the driver's
+    // operands through the tensor memory accelerator when the CUDA driver's
     // tensor-map encoder is available (the row stride K*2 is a multiple of
     // 16 bytes and both bases 16-byte aligned, as TMA requires)
     {

@@ -146,12 +146,15 @@ __device__ __forceinline__ float silu_grad(float z) {
     return s * (1.0f + z * (1.0f - s));
 }
 
-// inputs -> bf16 [B x 64] (columns >= 7 zero) and targets
-__global__ void mlp_gather(const float* X, const float* Y, const uint32_t* idx, int B, int n_valid,
-                           __nv_bfloat16* X0, float* t) {
+// inputs -> bf16 [B x 64] (columns >= 7 zero) and targets.  idx holds the
+// batch's dataset rows (null: rows 0..n_valid-1); with `iter` set, idx is a
+// ring of `ring` batches of n_valid rows and the batch is number *iter mod ring
+__global__ void mlp_gather(const float* X, const float* Y, const uint32_t* idx, const long long* iter, int ring,
+                           int B, int n_valid, __nv_bfloat16* X0, float* t) {
     const int b = blockIdx.x;
     const int c = threadIdx.x;   // 64 threads
     const bool valid = b < n_valid;
+    if (iter) idx += (*iter % ring) * (long long)n_valid;
     const long long s = valid ? (long long)(idx ? idx[b] : (uint32_t)b) : 0;
     const float v = (valid && c < MLP_IN) ? X[s * MLP_IN + c] : 0.0f;
     X0[(long long)b * MLP_K0 + c] = __float2bfloat16_rn(v);
@@ -218,35 +221,61 @@ __global__ void mlp_transpose(const __nv_bfloat16* in, int rows, int cols, __nv_
     }
 }
 
-// column sums: db[j] = sum_b dZ[b][j]  (fp32)
+// Column sums over the batch in a fixed order (deterministic): a 32 x 32
+// block covers 32 columns, thread row y sums batch rows y, y+32, ..., then
+// row 0 adds the 32 partial sums.  Each column is read as 128-byte lines.
+constexpr int kSumRows = 32;
+
+// db[j] = sum_b dZ[b][j]  (fp32)
 __global__ void mlp_colsum(const float* dZ, int B, int cols, float* db) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= cols) return;
+    __shared__ float part[kSumRows][33];
+    const int j = blockIdx.x * 32 + threadIdx.x;
     float s = 0.0f;
-    for (int b = 0; b < B; b++) s += dZ[(long long)b * cols + j];
-    db[j] = s;
+    if (j < cols)
+        for (int b = threadIdx.y; b < B; b += kSumRows) s += dZ[(long long)b * cols + j];
+    part[threadIdx.y][threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.y == 0 && j < cols) {
+        float t = 0.0f;
+        for (int k = 0; k < kSumRows; k++) t += part[k][threadIdx.x];
+        db[j] = t;
+    }
 }
 
-// dw5[j] = sum_b dy_b H4[b][j] ; db5 = sum_b dy_b
+// dw5[j] = sum_b dy_b H4[b][j] (blocks 0..7, as mlp_colsum); db5 = sum_b dy_b
+// (the last block: thread (x, y) sums rows y*32+x + 1024 k, then a fixed tree)
 __global__ void mlp_out_wgrad(const float* dy, const __nv_bfloat16* H4, int B, float* dw5, float* db5) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < MLP_H) {
-        float s = 0.0f;
-        for (int b = 0; b < B; b++) s += dy[b] * __bfloat162float(H4[(long long)b * MLP_H + j]);
-        dw5[j] = s;
+    __shared__ float part[kSumRows][33];
+    const bool bias = blockIdx.x == gridDim.x - 1;
+    const int j = blockIdx.x * 32 + threadIdx.x;
+    float s = 0.0f;
+    if (bias) {
+        for (int b = threadIdx.y * 32 + threadIdx.x; b < B; b += 32 * kSumRows) s += dy[b];
+    } else {
+        for (int b = threadIdx.y; b < B; b += kSumRows) s += dy[b] * __bfloat162float(H4[(long long)b * MLP_H + j]);
     }
-    if (j == 0) {
-        float s = 0.0f;
-        for (int b = 0; b < B; b++) s += dy[b];
-        db5[0] = s;
+    part[threadIdx.y][threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.y != 0) return;
+    float t = 0.0f;
+    for (int k = 0; k < kSumRows; k++) t += part[k][threadIdx.x];
+    if (!bias) {
+        dw5[j] = t;
+        return;
     }
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) db5[0] = t;
 }
 
-// Adam (Kingma & Ba 2015) with bias correction on the flat parameters
+// Adam (Kingma & Ba 2015) with bias correction on the flat parameters; the
+// step number is the device counter *step + 1 (the counter moves in
+// mlp_step_end, so a captured training step replays unchanged)
 __global__ void mlp_adam(float* p, const float* g, float* m, float* v, long long n, float lr, float b1, float b2,
-                         float eps, float c1, float c2) {
+                         float eps, const long long* step) {
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const float k = (float)(*step + 1);
+    const float c1 = 1.0f - powf(b1, k), c2 = 1.0f - powf(b2, k);
     const float gi = g[i];
     const float mi = b1 * m[i] + (1.0f - b1) * gi;
     const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
@@ -263,6 +292,13 @@ __global__ void mlp_weights_bf16(const float* W, int rows, int cols, __nv_bfloat
     const __nv_bfloat16 x = __float2bfloat16_rn(W[i]);
     Wb[i] = x;
     WTb[(long long)c * rows + r] = x;
+}
+
+// end of a training step: the step's mean loss, then both counters advance
+__global__ void mlp_step_end(const float* loss, float n_valid, long long* ctr, float* losses) {
+    losses[ctr[0]] = *loss / n_valid;
+    ctr[0]++;
+    ctr[1]++;
 }
 
 }  // namespace
@@ -287,7 +323,7 @@ struct pticm_mlp {
     float *dX = nullptr, *dY = nullptr;   // dataset on the device
     uint32_t* idx = nullptr;
     size_t data_n = 0;
-    long long step = 0;
+    long long* ctr = nullptr;         // device: [0] iteration of the current training call, [1] Adam steps taken
     DevStatus* status = nullptr;
     int* abort_flag = nullptr;
     std::vector<void*> allocs;
@@ -307,10 +343,11 @@ struct pticm_mlp {
 
 namespace {
 
-int mlp_refresh_bf16(pticm_mlp* m) {
+int mlp_refresh_bf16(pticm_mlp* m, cudaStream_t st) {
     for (int l = 0; l < MLP_LAYERS; l++) {
         const long long cnt = (long long)MLP_H * kKin[l];
-        mlp_weights_bf16<<<(unsigned)((cnt + 255) / 256), 256>>>(m->P + kWoff[l], MLP_H, kKin[l], m->Wb[l], m->WTb[l]);
+        mlp_weights_bf16<<<(unsigned)((cnt + 255) / 256), 256, 0, st>>>(m->P + kWoff[l], MLP_H, kKin[l], m->Wb[l],
+                                                                        m->WTb[l]);
     }
     MLP_CK(cudaGetLastError());
     return PTICM_OK;
@@ -324,42 +361,43 @@ int mlp_check_status(pticm_mlp* m) {
 }
 
 // forward for rows [0, n) of the staged batch; Z and H kept for backward
-int mlp_forward(pticm_mlp* m, int n_valid, bool with_loss) {
+int mlp_forward(pticm_mlp* m, int n_valid, bool with_loss, cudaStream_t st) {
     const int B = m->B;
     const __nv_bfloat16* in = m->X0;
     for (int l = 0; l < MLP_LAYERS; l++) {
         MLP_CK(tc_gemm(in, m->Wb[l], B, MLP_H, kKin[l], m->P + kBoff[l], 1, m->Z[l], m->H[l], MLP_H, m->status,
-                       m->abort_flag, nullptr));
+                       m->abort_flag, st));
         in = m->H[l];
     }
-    if (with_loss) MLP_CK(cudaMemset(m->loss, 0, sizeof(float)));
-    mlp_out_fwd<<<B / 8, 256>>>(m->H[3], m->P + kW5, m->P + kB5, m->t, n_valid, m->y, with_loss ? m->dy : nullptr,
+    if (with_loss) MLP_CK(cudaMemsetAsync(m->loss, 0, sizeof(float), st));
+    mlp_out_fwd<<<B / 8, 256, 0, st>>>(m->H[3], m->P + kW5, m->P + kB5, m->t, n_valid, m->y, with_loss ? m->dy : nullptr,
                                 with_loss ? m->loss : nullptr);
     MLP_CK(cudaGetLastError());
     return PTICM_OK;
 }
 
-int mlp_backward(pticm_mlp* m) {
+int mlp_backward(pticm_mlp* m, cudaStream_t st) {
     const int B = m->B;
     const dim3 tb(32, 8);
     // transposes of the layer inputs X0, H1, H2, H3
     const __nv_bfloat16* ins[MLP_LAYERS] = {m->X0, m->H[0], m->H[1], m->H[2]};
     for (int l = 0; l < MLP_LAYERS; l++)
-        mlp_transpose<<<dim3((kKin[l] + 31) / 32, (B + 31) / 32), tb>>>(ins[l], B, kKin[l], m->HT[l]);
-    mlp_out_wgrad<<<1, MLP_H>>>(m->dy, m->H[3], B, m->G + kW5, m->G + kB5);
+        mlp_transpose<<<dim3((kKin[l] + 31) / 32, (B + 31) / 32), tb, 0, st>>>(ins[l], B, kKin[l], m->HT[l]);
+    const dim3 sb(32, kSumRows);
+    mlp_out_wgrad<<<MLP_H / 32 + 1, sb, 0, st>>>(m->dy, m->H[3], B, m->G + kW5, m->G + kB5);
     const long long elems = (long long)B * MLP_H;
-    mlp_out_bwd<<<(unsigned)((elems + 255) / 256), 256>>>(m->dy, m->P + kW5, m->Z[3], B, m->dZf, m->dZ, m->dZT);
+    mlp_out_bwd<<<(unsigned)((elems + 255) / 256), 256, 0, st>>>(m->dy, m->P + kW5, m->Z[3], B, m->dZf, m->dZ, m->dZT);
     MLP_CK(cudaGetLastError());
     for (int l = MLP_LAYERS - 1; l >= 0; l--) {
         // dW_l = dZ_l^T . X_l  (M = 256 outputs, N = inputs, K = batch)
         MLP_CK(tc_gemm(m->dZT, m->HT[l], MLP_H, kKin[l], B, nullptr, 0, m->G + kWoff[l], nullptr, kKin[l], m->status,
-                       m->abort_flag, nullptr));
-        mlp_colsum<<<1, MLP_H>>>(m->dZf, B, MLP_H, m->G + kBoff[l]);
+                       m->abort_flag, st));
+        mlp_colsum<<<MLP_H / 32, sb, 0, st>>>(m->dZf, B, MLP_H, m->G + kBoff[l]);
         if (l == 0) break;
         // dH_{l-1} = dZ_l . W_l  (B = W_l^T as [inputs x outputs])
         MLP_CK(tc_gemm(m->dZ, m->WTb[l], B, kKin[l], MLP_H, nullptr, 0, m->dH, nullptr, kKin[l], m->status,
-                       m->abort_flag, nullptr));
-        mlp_silu_bwd<<<(unsigned)((elems + 255) / 256), 256>>>(m->dH, m->Z[l - 1], B, m->dZf, m->dZ, m->dZT);
+                       m->abort_flag, st));
+        mlp_silu_bwd<<<(unsigned)((elems + 255) / 256), 256, 0, st>>>(m->dH, m->Z[l - 1], B, m->dZf, m->dZ, m->dZT);
         MLP_CK(cudaGetLastError());
     }
     return PTICM_OK;
@@ -401,6 +439,7 @@ int pticm_mlp_create(uint64_t seed, uint32_t batch, pticm_mlp** out) {
     bad |= m->alloc(&m->idx, B) != cudaSuccess;
     bad |= m->alloc(&m->status, 1) != cudaSuccess;
     bad |= m->alloc(&m->abort_flag, 1) != cudaSuccess;
+    bad |= m->alloc(&m->ctr, 2) != cudaSuccess;
     if (bad) {
         delete m;
         return mlp_fail(PTICM_ERR_NOMEM, "device allocation failed");
@@ -428,7 +467,7 @@ int pticm_mlp_create(uint64_t seed, uint32_t batch, pticm_mlp** out) {
                 p[kWoff[l] + (size_t)r * kKin[l] + c] = (l == 0 && c >= MLP_IN) ? 0.0f : sc * gauss();
     }
     for (int j = 0; j < MLP_H; j++) p[kW5 + j] = std::sqrt(1.0f / MLP_H) * gauss();
-    if (cudaMemcpy(m->P, p.data(), kParams * 4, cudaMemcpyHostToDevice) != cudaSuccess || mlp_refresh_bf16(m)) {
+    if (cudaMemcpy(m->P, p.data(), kParams * 4, cudaMemcpyHostToDevice) != cudaSuccess || mlp_refresh_bf16(m, 0)) {
         delete m;
         return mlp_fail(PTICM_ERR_CUDA, "parameter upload failed");
     }
@@ -449,7 +488,7 @@ int pticm_mlp_get_params(pticm_mlp* m, float* out) {
 int pticm_mlp_set_params(pticm_mlp* m, const float* in) {
     if (!m || !in) return mlp_fail(PTICM_ERR_INVALID, "null argument");
     MLP_CK(cudaMemcpy(m->P, in, kParams * 4, cudaMemcpyHostToDevice));
-    return mlp_refresh_bf16(m);
+    return mlp_refresh_bf16(m, 0);
 }
 
 int pticm_mlp_set_data(pticm_mlp* m, const float* x, const float* y, uint64_t n) {
@@ -468,10 +507,10 @@ int pticm_mlp_gradients(pticm_mlp* m, const float* x, const float* y, uint32_t n
     if (!m || !x || !y || n == 0 || (int)n > m->B) return mlp_fail(PTICM_ERR_INVALID, "invalid arguments");
     if (int rc = pticm_mlp_set_data(m, x, y, n)) return rc;
     MLP_CK(cudaMemset(m->status, 0, sizeof(DevStatus)));
-    mlp_gather<<<m->B, MLP_K0>>>(m->dX, m->dY, nullptr, m->B, (int)n, m->X0, m->t);
+    mlp_gather<<<m->B, MLP_K0>>>(m->dX, m->dY, nullptr, nullptr, 1, m->B, (int)n, m->X0, m->t);
     MLP_CK(cudaGetLastError());
-    if (int rc = mlp_forward(m, (int)n, true)) return rc;
-    if (int rc = mlp_backward(m)) return rc;
+    if (int rc = mlp_forward(m, (int)n, true, 0)) return rc;
+    if (int rc = mlp_backward(m, 0)) return rc;
     MLP_CK(cudaDeviceSynchronize());
     if (int rc = mlp_check_status(m)) return rc;
     if (grads) MLP_CK(cudaMemcpy(grads, m->G, kParams * 4, cudaMemcpyDeviceToHost));
@@ -485,11 +524,18 @@ int pticm_mlp_gradients(pticm_mlp* m, const float* x, const float* y, uint32_t n
 
 int pticm_mlp_train(pticm_mlp* m, const float* x, const float* y, uint64_t n, uint32_t steps, float lr,
                     uint64_t seed, float* loss_per_step) {
-    if (!m || !x || !y || n == 0) return mlp_fail(PTICM_ERR_INVALID, "invalid arguments");
+    if (!m || !x || !y || n == 0 || n > 0xFFFFFFFFull) return mlp_fail(PTICM_ERR_INVALID, "invalid arguments");
     if (int rc = pticm_mlp_set_data(m, x, y, n)) return rc;
-    MLP_CK(cudaMemset(m->status, 0, sizeof(DevStatus)));
+    if (steps == 0) return PTICM_OK;
     const int B = m->B;
     const int nb = (int)std::min<uint64_t>(n, (uint64_t)B);
+    // Batches: an epoch-wise Fisher-Yates shuffle on the host (xorshift64),
+    // written a chunk of kChunk steps at a time into one half of a pinned
+    // two-chunk ring; the device ring (the same layout) is read by the
+    // captured step at row (iteration mod 2 kChunk).  The host fills chunk
+    // c + 2 while chunk c + 1 runs.
+    constexpr uint32_t kChunk = 256;
+    const size_t half = (size_t)kChunk * nb;
     std::vector<uint32_t> order(n);
     for (uint64_t i = 0; i < n; i++) order[i] = (uint32_t)i;
     uint64_t s = seed ^ 0xA0761D6478BD642Full;
@@ -498,31 +544,76 @@ int pticm_mlp_train(pticm_mlp* m, const float* x, const float* y, uint64_t n, ui
         return s;
     };
     uint64_t cursor = n;
-    std::vector<uint32_t> batch(B, 0);
-    for (uint32_t it = 0; it < steps; it++) {
-        for (int b = 0; b < nb; b++) {
+    auto fill = [&](uint32_t* dst, uint32_t count) {
+        for (size_t k = 0; k < (size_t)count * nb; k++) {
             if (cursor == n) {   // reshuffle each epoch
                 for (uint64_t i = n - 1; i > 0; i--) std::swap(order[i], order[nxt() % (i + 1)]);
                 cursor = 0;
             }
-            batch[b] = order[cursor++];
+            dst[k] = order[cursor++];
         }
-        MLP_CK(cudaMemcpy(m->idx, batch.data(), (size_t)nb * 4, cudaMemcpyHostToDevice));
-        mlp_gather<<<B, MLP_K0>>>(m->dX, m->dY, m->idx, B, nb, m->X0, m->t);
-        if (int rc = mlp_forward(m, nb, true)) return rc;
-        if (int rc = mlp_backward(m)) return rc;
-        m->step++;
-        const float c1 = 1.0f - std::pow(0.9f, (float)m->step), c2 = 1.0f - std::pow(0.999f, (float)m->step);
-        mlp_adam<<<(unsigned)((kParams + 255) / 256), 256>>>(m->P, m->G, m->Mm, m->Vm, (long long)kParams, lr, 0.9f,
-                                                             0.999f, 1e-8f, c1, c2);
-        if (int rc = mlp_refresh_bf16(m)) return rc;
-        if (loss_per_step) {
-            float l = 0;
-            MLP_CK(cudaMemcpy(&l, m->loss, 4, cudaMemcpyDeviceToHost));
-            loss_per_step[it] = l / (float)nb;
+    };
+
+    struct Res {
+        cudaStream_t st = nullptr;
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        uint32_t* ring = nullptr;    // device, 2 kChunk batches
+        uint32_t* hring = nullptr;   // pinned host
+        float* losses = nullptr;     // device, one per step
+        cudaEvent_t copied[2] = {nullptr, nullptr};
+        ~Res() {
+            if (st) cudaStreamSynchronize(st);
+            if (exec) cudaGraphExecDestroy(exec);
+            if (graph) cudaGraphDestroy(graph);
+            for (cudaEvent_t e : copied)
+                if (e) cudaEventDestroy(e);
+            if (st) cudaStreamDestroy(st);
+            cudaFree(ring);
+            cudaFree(losses);
+            cudaFreeHost(hring);
         }
+    } r;
+    MLP_CK(cudaStreamCreateWithFlags(&r.st, cudaStreamNonBlocking));
+    MLP_CK(cudaMalloc(&r.ring, 2 * half * 4));
+    MLP_CK(cudaMalloc(&r.losses, (size_t)steps * 4));
+    MLP_CK(cudaMallocHost(&r.hring, 2 * half * 4));
+    for (cudaEvent_t& e : r.copied) MLP_CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    MLP_CK(cudaMemsetAsync(m->status, 0, sizeof(DevStatus), r.st));
+    MLP_CK(cudaMemsetAsync(m->ctr, 0, sizeof(long long), r.st));   // this call's iteration counter
+
+    // one training step, captured once: gather, forward with loss, backward,
+    // Adam, bf16 weight copies, counters (37 kernels and one memset)
+    MLP_CK(cudaStreamBeginCapture(r.st, cudaStreamCaptureModeRelaxed));
+    int rc = PTICM_OK;
+    mlp_gather<<<B, MLP_K0, 0, r.st>>>(m->dX, m->dY, r.ring, m->ctr, 2 * (int)kChunk, B, nb, m->X0, m->t);
+    if (!rc) rc = mlp_forward(m, nb, true, r.st);
+    if (!rc) rc = mlp_backward(m, r.st);
+    if (!rc) {
+        mlp_adam<<<(unsigned)((kParams + 255) / 256), 256, 0, r.st>>>(m->P, m->G, m->Mm, m->Vm, (long long)kParams,
+                                                                       lr, 0.9f, 0.999f, 1e-8f, m->ctr + 1);
+        rc = mlp_refresh_bf16(m, r.st);
     }
-    MLP_CK(cudaDeviceSynchronize());
+    if (!rc) mlp_step_end<<<1, 1, 0, r.st>>>(m->loss, (float)nb, m->ctr, r.losses);
+    const cudaError_t ec = cudaStreamEndCapture(r.st, &r.graph);
+    if (rc) return rc;
+    MLP_CK(ec);
+    MLP_CK(cudaGraphInstantiate(&r.exec, r.graph, 0));
+
+    for (uint32_t c0 = 0, chunk = 0; c0 < steps; c0 += kChunk, chunk++) {
+        const uint32_t cnt = std::min(kChunk, steps - c0);
+        const int h = (int)(chunk & 1);
+        // the pinned half is free once its previous upload (two chunks ago) ran
+        MLP_CK(cudaEventSynchronize(r.copied[h]));
+        fill(r.hring + h * half, cnt);
+        MLP_CK(cudaMemcpyAsync(r.ring + h * half, r.hring + h * half, (size_t)cnt * nb * 4, cudaMemcpyHostToDevice,
+                               r.st));
+        MLP_CK(cudaEventRecord(r.copied[h], r.st));
+        for (uint32_t i = 0; i < cnt; i++) MLP_CK(cudaGraphLaunch(r.exec, r.st));
+    }
+    if (loss_per_step)
+        MLP_CK(cudaMemcpyAsync(loss_per_step, r.losses, (size_t)steps * 4, cudaMemcpyDeviceToHost, r.st));
+    MLP_CK(cudaStreamSynchronize(r.st));
     return mlp_check_status(m);
 }
 
@@ -538,8 +629,8 @@ int pticm_mlp_predict(pticm_mlp* m, const float* x, uint64_t n, float* y) {
         const int nb = (int)std::min<uint64_t>((uint64_t)B, n - base);
         for (int b = 0; b < nb; b++) batch[b] = (uint32_t)(base + b);
         MLP_CK(cudaMemcpy(m->idx, batch.data(), (size_t)nb * 4, cudaMemcpyHostToDevice));
-        mlp_gather<<<B, MLP_K0>>>(m->dX, m->dY, m->idx, B, nb, m->X0, m->t);
-        if (int rc = mlp_forward(m, nb, false)) return rc;
+        mlp_gather<<<B, MLP_K0>>>(m->dX, m->dY, m->idx, nullptr, 1, B, nb, m->X0, m->t);
+        if (int rc = mlp_forward(m, nb, false, 0)) return rc;
         MLP_CK(cudaMemcpy(y + base, m->y, (size_t)nb * 4, cudaMemcpyDeviceToHost));
     }
     return mlp_check_status(m);

@@ -4,7 +4,8 @@ CPU: the oracle's FP64 backward pass agrees with central finite differences
 (pins the oracle), and its bf16 rounding helper is round-to-nearest-even.
 GPU: the tensor-core gradients equal the oracle's (same bf16 rounding
 points) within 1e-2 relative L2 per parameter block and the loss within
-1e-3; Adam training lowers the loss; prediction is batch-size independent.
+1e-3; the captured training step applies Adam as the oracle's gradients
+give it; training lowers the loss; prediction is batch-size independent.
 """
 import numpy as np
 import pytest
@@ -67,6 +68,36 @@ def test_tensor_core_gradients_match_oracle(n):
             b = b.reshape(MO.H, MO.K0)[:, :MO.IN]
         err = np.linalg.norm(a - b) / (np.linalg.norm(b) + 1e-30)
         assert err < 1e-2, (key, err)
+
+
+@pytest.mark.gpu
+def test_captured_adam_steps_match_oracle_adam():
+    """Three one-step training calls on a dataset smaller than the batch (each
+    step sees every row): the captured step's update equals Adam applied to
+    the oracle's gradients at the device's parameters, with the bias
+    corrections of steps 1, 2, 3 (the step counter outlives a call)."""
+    import pticm
+    rng = np.random.default_rng(4)
+    n, lr = 300, 1e-3
+    X = rng.standard_normal((n, MO.IN)).astype(np.float32)
+    t = rng.standard_normal(n).astype(np.float32)
+    m = pticm.MLP(seed=2, batch=1024)
+    m.params = MO.init_like_device(13).astype(np.float32)
+    mom = np.zeros(MO.PARAM_COUNT)
+    vel = np.zeros(MO.PARAM_COUNT)
+    for k in range(1, 4):
+        p0 = m.params.astype(np.float64)
+        ol, g = MO.loss_and_grad(p0, X, t, emulate_bf16=True)
+        losses = m.train(X, t, steps=1, lr=lr, seed=k)
+        assert abs(losses[0] - ol) <= 1e-3 * abs(ol)
+        mom = 0.9 * mom + 0.1 * g
+        vel = 0.999 * vel + 0.001 * g * g
+        want = -lr * (mom / (1 - 0.9 ** k)) / (np.sqrt(vel / (1 - 0.999 ** k)) + 1e-8)
+        got = m.params.astype(np.float64) - p0
+        err = np.abs(got - want) / lr
+        # gradients agree to ~1e-2; entries with near-zero gradient may differ
+        assert np.median(err) < 0.02, (k, np.median(err))
+        assert np.mean(err < 0.25) > 0.97, (k, np.mean(err < 0.25))
 
 
 @pytest.mark.gpu

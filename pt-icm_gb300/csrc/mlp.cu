@@ -58,12 +58,12 @@ extern "C" int pticm_tc_gemm_check(int M, int N, int K, const uint16_t* A, const
         cleanup();
         return mlp_fail(PTICM_ERR_NOMEM, "device allocation failed");
     }
-    cudaMemcpy(dA, A, (size_t)M * K * 2, cudaMemcpyHostToDevice);
-    cudaMemcpy(dB, B, (size_t)N * K * 2, cudaMemcpyHostToDevice);
-    if (bias) cudaMemcpy(db, bias, (size_t)N * 4, cudaMemcpyHostToDevice);
-    cudaMemset(ds, 0, sizeof(DevStatus));
-    cudaMemset(dab, 0, 4);
-    cudaError_t e = tc_gemm(dA, dB, M, N, K, db, act, dC, nullptr, N, ds, dab, nullptr);
+    cudaError_t e = cudaMemcpy(dA, A, (size_t)M * K * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dB, B, (size_t)N * K * 2, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && bias) e = cudaMemcpy(db, bias, (size_t)N * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(ds, 0, sizeof(DevStatus));
+    if (e == cudaSuccess) e = cudaMemset(dab, 0, 4);
+    if (e == cudaSuccess) e = tc_gemm(dA, dB, M, N, K, db, act, dC, nullptr, N, ds, dab, nullptr);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     DevStatus hs{};
     if (e == cudaSuccess) e = cudaMemcpy(&hs, ds, sizeof hs, cudaMemcpyDeviceToHost);
@@ -94,13 +94,13 @@ extern "C" int pticm_tc_gemm_bench(int M, int N, int K, int iters, double* ms_pe
         cleanup();
         return mlp_fail(PTICM_ERR_NOMEM, "device allocation failed");
     }
-    cudaMemset(dA, 0x3c, (size_t)M * K * 2);   // bf16 ~1.0 everywhere: finite sums
-    cudaMemset(dB, 0x3c, (size_t)N * K * 2);
-    cudaMemset(ds, 0, sizeof(DevStatus));
-    cudaMemset(dab, 0, 4);
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    cudaError_t e = tc_gemm(dA, dB, M, N, K, nullptr, 0, nullptr, dC, N, ds, dab, nullptr);   // warm-up
+    cudaError_t e = cudaMemset(dA, 0x3c, (size_t)M * K * 2);   // bf16 ~1.0 everywhere: finite sums
+    if (e == cudaSuccess) e = cudaMemset(dB, 0x3c, (size_t)N * K * 2);
+    if (e == cudaSuccess) e = cudaMemset(ds, 0, sizeof(DevStatus));
+    if (e == cudaSuccess) e = cudaMemset(dab, 0, 4);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) e = tc_gemm(dA, dB, M, N, K, nullptr, 0, nullptr, dC, N, ds, dab, nullptr);   // warm-up
     if (e == cudaSuccess) e = cudaEventRecord(e0, nullptr);
     for (int i = 0; i < iters && e == cudaSuccess; i++)
         e = tc_gemm(dA, dB, M, N, K, nullptr, 0, nullptr, dC, N, ds, dab, nullptr);

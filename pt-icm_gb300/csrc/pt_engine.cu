@@ -497,6 +497,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                         // S never outgrows the free part of lst: |S| <= llen <= n - llen
                         const int pos = atomicAdd(team.ctl + 4, 1);
                         if (pos < llen) lst[sbase + pos] = u;
+                        return;
                     }
                     const int e1 = B.row[u + 1];
 #pragma unroll 4
@@ -506,6 +507,25 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                     }
                 });
                 team.sync();
+                if (BLOCK) {
+                    // the edges of S: one warp per site and one lane per
+                    // neighbour (the unions of a site side by side) when
+                    // that takes fewer rounds than one thread per site
+                    const int ns0 = min(*(volatile int*)(team.ctl + 4), llen);
+                    const int nw = team.ts >> 5;
+                    const bool by_warp = (ns0 + nw - 1) / nw < (D.nnz + n - 1) / n;
+                    const int t0 = by_warp ? team.tr >> 5 : team.tr, dt = by_warp ? nw : team.ts;
+                    const int a0 = by_warp ? team.tr & 31 : 0, da = by_warp ? 32 : 1;
+                    for (int t = t0; t < ns0; t += dt) {
+                        const int u = lst[sbase + t];
+                        const int e1 = B.row[u + 1];
+                        for (int a = B.row[u] + a0; a < e1; a += da) {
+                            const int v = (int)(B.adj[a] >> 8);
+                            if (d[v]) ok &= uf_unite(lab, u, v);
+                        }
+                    }
+                    team.sync();
+                }
                 if (BLOCK) {
                     // sites in L's component at their phase-3 check stay in it:
                     // every site outside the final component of L is in S

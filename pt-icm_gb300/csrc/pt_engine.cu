@@ -629,14 +629,22 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
         // its neighbours; the energy changes by the edges leaving the flipped
         // set F.  F is a union of overlap components, so a neighbour outside
         // F is outside the overlap (equal in A and B) and keeps its spin.
-        auto flip_push = [&](int u) {
+        // (by_warp: the lanes of a warp share the site, read its spins
+        // before lane 0 flips them and take every 32nd edge)
+        auto flip_push = [&](int u, bool by_warp) {
             const int hu = D.has_h ? B.h[u] : 0;
+            const int lane = by_warp ? (threadIdx.x & 31) : 0;
             int sa = 0, sb = 0;   // spins before the flip
-            if (locA) { sa = sA[u]; sA[u] = (int8_t)-sa; dEa -= 2 * sa * hu; }
-            if (locB) { sb = sB[u]; sB[u] = (int8_t)-sb; dEb -= 2 * sb * hu; }
-            const int e1 = B.row[u + 1];
+            if (locA) sa = sA[u];
+            if (locB) sb = sB[u];
+            if (by_warp) __syncwarp();
+            if (lane == 0) {
+                if (locA) { sA[u] = (int8_t)-sa; dEa -= 2 * sa * hu; }
+                if (locB) { sB[u] = (int8_t)-sb; dEb -= 2 * sb * hu; }
+            }
+            const int e1 = B.row[u + 1], da = by_warp ? 32 : 1;
 #pragma unroll 4
-            for (int a = B.row[u]; a < e1; a++) {
+            for (int a = B.row[u] + lane; a < e1; a += da) {
                 const uint32_t e = B.adj[a];
                 const int v = (int)(e >> 8);
                 const int J = (int)(int8_t)(e & 0xffu);
@@ -650,9 +658,14 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
             }
         };
         if (fast) {
-            for (int t = team.tr; t < ns; t += team.ts) {
+            // one warp per site when that takes fewer rounds (as for the
+            // unions of S); the membership test is the same in every lane
+            const int nw = team.ts >> 5;
+            const bool by_warp = BLOCK && (ns + nw - 1) / nw < (D.nnz + n - 1) / n;
+            const int t0 = by_warp ? team.tr >> 5 : team.tr, dt = by_warp ? nw : team.ts;
+            for (int t = t0; t < ns; t += dt) {
                 const int u = lst[sbase + t];
-                if ((uf_find((volatile int*)X.queue, u) == fast_root) == fast_eq) flip_push(u);
+                if ((uf_find((volatile int*)X.queue, u) == fast_root) == fast_eq) flip_push(u, by_warp);
             }
         } else if (BLOCK && fsize * 4 > (long long)n) {
             // a large cluster: flip, then fields and energies from scratch
@@ -688,7 +701,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
         } else {
             // a small flipped set, flipped and pushed in one pass
             for_overlap([&](int u) {
-                if (in_flip(u)) flip_push(u);
+                if (in_flip(u)) flip_push(u, false);
             });
         }
         team.sync();

@@ -436,16 +436,22 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                 // is in L too -- then both are already joined.
                 for (int round = 0; round < 2; round++) {
                     for_overlap([&](int u) {
-                        int k = 0;
+                        // the neighbour list four entries at a time: four
+                        // independent loads, then four flag loads
+                        int k = 0, tgt = -1;
                         const int e1 = B.row[u + 1];
-                        for (int a = B.row[u]; a < e1; a++) {
-                            const int v = (int)(B.adj[a] >> 8);
-                            if (!d[v]) continue;
-                            if (k++ == round) {
-                                ok &= uf_unite(lab, u, v);
-                                break;
-                            }
+                        for (int a = B.row[u]; a < e1 && tgt < 0; a += 4) {
+                            int v[4];
+                            bool on[4];
+#pragma unroll
+                            for (int j = 0; j < 4; j++) v[j] = a + j < e1 ? (int)(B.adj[a + j] >> 8) : u;
+#pragma unroll
+                            for (int j = 0; j < 4; j++) on[j] = a + j < e1 && d[v[j]];
+#pragma unroll
+                            for (int j = 0; j < 4; j++)
+                                if (on[j] && tgt < 0 && k++ == round) tgt = v[j];
                         }
+                        if (tgt >= 0) ok &= uf_unite(lab, u, tgt);
                     });
                     team.sync();
                     if (round == 0) {

@@ -83,6 +83,12 @@ PTICM_API int pticm_problem_from_dense(int64_t n, const double* J, const double*
 PTICM_API void pticm_problem_free(pticm_problem* p);
 PTICM_API int pticm_problem_get_info(const pticm_problem* p, pticm_problem_info* out);
 
+/* The sweep's colour class of every site (original numbering), n entries.
+ * The engine updates a class in parallel, so no edge may join two sites of
+ * one class; the classes come from a two-colouring of bipartite graphs, else
+ * the better of Welsh-Powell and DSatur.  Host only (no device work). */
+PTICM_API int pticm_problem_get_colouring(const pticm_problem* p, int32_t* colour);
+
 /* Problem::energy, Problem::maxcut, Problem::calculate_dE
  * src/problem.cc:33-162, computed on the GPU for `count` states
  * (count*n bytes).  `dE` (count*n doubles) may be NULL. */

@@ -798,6 +798,14 @@ int pticm_problem_get_info(const pticm_problem* p, pticm_problem_info* out) {
     return PTICM_OK;
 }
 
+int pticm_problem_get_colouring(const pticm_problem* p, int32_t* colour) {
+    if (!p || !colour) return fail(PTICM_ERR_INVALID, "null argument");
+    const HostProblem& P = p->hp;
+    for (int32_t c = 0; c < P.ncolors; c++)
+        for (int32_t d = P.color_off[c]; d < P.color_off[c + 1]; d++) colour[P.perm[d]] = c;
+    return PTICM_OK;
+}
+
 int pticm_problem_evaluate(const pticm_problem* pc, int64_t count, const uint8_t* states, double* energy,
                            double* maxcut, double* dE) {
     if (!pc || count < 0 || (count > 0 && !states)) return fail(PTICM_ERR_INVALID, "invalid arguments");

@@ -78,6 +78,7 @@ def lib():
         "pticm_problem_from_coo": [i64, i64, P, P, P, P, C.POINTER(P)],
         "pticm_problem_from_dense": [i64, P, P, C.POINTER(P)],
         "pticm_problem_get_info": [P, C.POINTER(ProblemInfo)],
+        "pticm_problem_get_colouring": [P, P],
         "pticm_problem_evaluate": [P, i64, P, P, P, P],
         "pticm_create": [P, C.POINTER(Opts), C.POINTER(P)],
         "pticm_set_ladder": [P, P, u32, i32],
@@ -213,6 +214,12 @@ class Problem:
     @property
     def n(self) -> int:
         return self.info().n
+
+    def colouring(self):
+        """The sweep's colour class of every site (host only)."""
+        out = np.zeros(self.n, np.int32)
+        _check(lib().pticm_problem_get_colouring(self._h, _p(out)))
+        return out
 
     def evaluate(self, states, with_dE=False):
         """Energy, max-cut and (optionally) dE of each state (rows of 0/1)."""

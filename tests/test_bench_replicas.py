@@ -1,5 +1,7 @@
-"""bench.py's replicas-only N>1 host logic on two gloo ranks (CPU): the job
-time is the slowest rank's, the throughput counts every rank's work."""
+"""bench.py's host logic on the CPU: the replicas-only N>1 path on two gloo
+ranks (the job time is the slowest rank's, the throughput counts every
+rank's work), and the reference arm's JSON line (rank 0 prints it, other
+ranks exit without work)."""
 import os
 import sys
 
@@ -44,3 +46,38 @@ def test_single_rank_is_identity():
     import bench
     assert bench.max_over_ranks(12.5) == 12.5
     assert bench.job_throughput(1, 10, 1000.0) == 10.0
+
+
+def _run_bench(args, env_extra=None):
+    import subprocess
+    env = dict(os.environ)
+    env.update(env_extra or {})
+    return subprocess.run([sys.executable, os.path.join(ROOT, "bench.py")] + args, cwd=ROOT, env=env,
+                          capture_output=True, text=True, timeout=600)
+
+
+def test_reference_arm_prints_one_contract_line():
+    """`bench.py --impl reference` on a tiny sample: one JSON line with the
+    contract's keys, the CPU baseline describing the run, e2e without copies."""
+    import json
+    r = _run_bench(["--impl", "reference", "--steps", "1", "--warmup", "0", "--ref-pts", "2"])
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference"
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in d, key
+    assert d["value"] > 0 and d["steps"] == 1 and d["higher_is_better"] is True
+    assert "workload" in d["config"]
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["cores"] >= 1 and cb["kind"] in ("port", "reference") and cb["sample"]
+    e = d["e2e"]
+    assert e["value"] == d["value"] and e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
+
+
+def test_reference_arm_other_ranks_exit_quietly():
+    r = _run_bench(["--impl", "reference", "--steps", "1", "--warmup", "0", "--ref-pts", "2"], {"RANK": "1"})
+    assert r.returncode == 0
+    assert r.stdout.strip() == ""

@@ -108,9 +108,11 @@ int main(int argc, char** argv) {
         }
         if (!help && problem_path.empty() && folder.empty()) throw std::runtime_error("--problem is required");
     } catch (const std::exception& e) {
+        // the reference prints the error and the usage too, then carries on
+        // with the empty path; here an argument error ends with status 1
         std::cout << e.what() << std::endl;
         usage();
-        return 0;
+        return 1;
     }
     if (help) {
         usage();

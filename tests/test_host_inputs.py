@@ -3,8 +3,10 @@
 The library's parser follows src/problem.cc:183-247: the header, the index
 base chosen by the file name, a missing weight meaning 1, blank lines
 skipped, the dense/sparse choice at 10 % density (duplicate lines are
-parallel edges in sparse files and overwrite in dense ones).  Each case is
-compared with the oracle's parse of the same file.  Inputs the engine cannot
+parallel edges in sparse files and overwrite in dense ones).  Each case, and
+each text-layout variant (CRLF, tabs, trailing blanks, no final newline, a
+header counting more edges than follow), is compared with the oracle's parse
+of the same file.  Inputs the engine cannot
 represent exactly are refused with a status code; the product has no CPU
 path, so creating a context without a GPU fails loudly.
 """
@@ -26,6 +28,18 @@ CASES = {
     "lin.ising": "3 2 1\n0 1\n2 -1\n0 1 2\n",
 }
 
+# text-layout variants, parsed on the host only
+LAYOUT_CASES = {
+    "short_header": "3 5\n1 2 1\n2 3 -1\n",        # fewer lines than the header's M (M still scales)
+    "crlf": "3 2\r\n1 2 1\r\n2 3 -1\r\n",
+    "tabs": "3 2\n1\t2\t1\n2\t3\t-1\n",
+    "trailing_space": "3 2\n1 2 1 \n2 3 -1   \n",
+    "blank_end": "3 2\n1 2 1\n2 3 -1\n\n\n",
+    "no_final_newline": "3 2\n1 2 1\n2 3 -1",
+    "plus_sign": "3 2\n1 2 +1\n2 3 -1\n",
+    "float_int": "3 2\n1 2 1.0\n2 3 -2.0\n",
+}
+
 REJECTED = {
     "selfloop": ("2 1\n1 1 1\n", 3),
     "fraction": ("2 1\n1 2 0.5\n", 3),
@@ -37,14 +51,14 @@ REJECTED = {
 
 def _write(tmp_path, name, text):
     p = tmp_path / name
-    p.write_text(text)
+    p.write_bytes(text.encode())   # line endings as given
     return str(p)
 
 
-@pytest.mark.parametrize("name", sorted(CASES))
+@pytest.mark.parametrize("name", sorted(CASES) + sorted(LAYOUT_CASES))
 def test_parse_matches_oracle(tmp_path, name):
     import pticm
-    path = _write(tmp_path, name, CASES[name])
+    path = _write(tmp_path, name, CASES.get(name) or LAYOUT_CASES[name])
     info = pticm.Problem.load(path).info()
     orc = O.Problem.load(path, 0)
     assert info.n == orc.n and info.m == orc.m

@@ -4,7 +4,9 @@
   draws from (tests/golden/rng_kat.json, made by tests/golden/rng_kat.cc);
 * against the reports of the unmodified reference built single-rank
   (tests/golden/ref_runs.json, made by tests/golden/make_golden.py);
-* live against that reference build when it exists on this host.
+* live against that reference build when it exists on this host (random
+  graphs, and dense, --preprocess, multi-sweep, inverse-temperature,
+  linear-term and larger configurations).
 """
 import json
 import os
@@ -100,6 +102,42 @@ def test_oracle_matches_reference_live(seed, tmp_path):
     kw = dict(seed=seed, Nt=6 + seed % 3, pts=120, icm=True, T0=0.4, T1=3.0)
     rep = O.run_reference(path, **kw)
     o = O.solve(O.Problem.load(path, seed), **kw)
+    _compare(rep, o)
+
+
+LIVE_CASES = [
+    # (instance factory, file name, solve arguments)
+    ("lattice6_dense_pre", lambda I: I.pm_lattice(6, seed=31), "l6.gset",
+     dict(seed=31, Nt=6, pts=80, icm=True, T0=0.5, T1=3.0, preprocess=True, pre_samples=200)),
+    ("lattice8_sweeps3", lambda I: I.pm_lattice(8, seed=32), "l8.gset",
+     dict(seed=32, Nt=7, pts=90, icm=False, T0=0.4, T1=2.6, sweeps=3)),
+    ("random_inverse", lambda I: I.random_graph(120, 500, seed=33, signed=True), "r120",
+     dict(seed=33, Nt=6, pts=100, icm=True, T0=0.3, T1=2.5, inverse=True)),
+    ("random500_deg10", lambda I: I.random_graph(500, 2500, seed=34, signed=False), "r500",
+     dict(seed=34, Nt=10, pts=60, icm=True, T0=0.5, T1=10.0)),
+    ("linear_terms", None, "lin.ising",
+     dict(seed=35, Nt=6, pts=100, icm=True, T0=0.5, T1=3.0)),
+]
+
+
+def _linear_instance(I):
+    inst = I.random_graph(50, 120, seed=35, signed=True)
+    inst.h = np.random.default_rng(35).choice(np.array([-2.0, -1.0, 0.0, 1.0, 2.0]), size=inst.n)
+    return inst
+
+
+@pytest.mark.skipif(not O.have_reference(), reason="reference build absent on this host")
+@pytest.mark.parametrize("case", LIVE_CASES, ids=[c[0] for c in LIVE_CASES])
+def test_oracle_matches_reference_live_configurations(case, tmp_path):
+    """Dense and sparse files, --preprocess, several sweeps, inverse
+    temperatures, linear terms and a larger graph, each run by the reference
+    build and by the oracle with the same seed."""
+    from pticm import instances as I
+    _, fac, fname, kw = case
+    inst = _linear_instance(I) if fac is None else fac(I)
+    path = inst.write_gset(str(tmp_path / fname))
+    rep = O.run_reference(path, **kw)
+    o = O.solve(O.Problem.load(path, kw["seed"]), **kw)
     _compare(rep, o)
 
 

@@ -126,7 +126,7 @@ PTICM_API void pticm_destroy(pticm_ctx* c);
  * top slot down while beta >= char_scale) unless `nc` >= 0 sets it. */
 PTICM_API int pticm_set_ladder(pticm_ctx* c, const double* beta, uint32_t nt, int32_t nc);
 
-/* beta_linspace (src/mpi_utils.cc:6-22), linear in beta, same FP64 steps. */
+/* beta_linspace (src/utils.cc:6-22), linear in beta, same FP64 steps. */
 PTICM_API int pticm_beta_linspace(double* beta, double T0, double T1, uint64_t nt, int inverse);
 
 /* initialize_replicas (src/initialization.cc:63-76): Bernoulli(1/2) spins
@@ -176,6 +176,46 @@ PTICM_API int pticm_get_replicas(pticm_ctx* c, uint8_t* states, int64_t* energy,
  * process from src/main.cc to the report). */
 PTICM_API int pticm_checkpoint_save(pticm_ctx* c, const char* path);
 PTICM_API int pticm_checkpoint_load(pticm_ctx* c, const char* path);
+
+/* One ICM phase on the current states with caller-chosen seeds: icm(w, k)
+ * (src/icm.cc:74-215) for every pair q = (c/2)*nc + (nt-1-k) of chains c,
+ * c+1 at temperature slot k, on the same kernel and block layout as
+ * pticm_run.  seeds[q] (count = nc * chains/2 entries) is the seed site in
+ * the original numbering -- the reference's xor_icm draw (src/icm.cc:33),
+ * which must lie where the pair differs after its global-flip rule
+ * (src/icm.cc:20-28) -- or -1 for the engine's own draw, or -2 to leave the
+ * pair alone.  exact = 1 flips the seed's cluster itself, as bfs_icm
+ * (src/icm.cc:37-72) does; exact = 0 flips the smaller of the cluster and the
+ * rest of the overlap, as production does (the two chains then hold each
+ * other's result).  Counts as one PT step of the random streams. */
+PTICM_API int pticm_icm_pairs(pticm_ctx* c, const int64_t* seeds, uint32_t count, int exact);
+
+/* The exchange order of the reference-order exchange (exchange = 0): the nt-1
+ * pair indices in the order the next attempts take them (chain_1_exchange_
+ * order of src/initialization.cc:77-100 and src/replica_exchange.cc:86-91). */
+PTICM_API int pticm_get_exchange_order(pticm_ctx* c, uint32_t* order);
+
+/* Bounded waits.  Every wait of a kernel on other blocks (the group barrier
+ * of a PT step) or on bulk copies gives up after limit_ns (0: the default,
+ * 2 s), records where, and the call returns PTICM_ERR_DEVICE; the context
+ * stays usable.  phantom_arrivals = 1 is a test hook: every group barrier
+ * then waits for one block more than it has, so each of its waits runs out
+ * (the reference has no failure detection: src/initialization.cc:120-126 and
+ * src/mpi_utils.cc:223-225 assert or exit). */
+PTICM_API int pticm_set_wait_limit(pticm_ctx* c, uint64_t limit_ns, uint32_t phantom_arrivals);
+
+/* The engine layout a context runs (chosen at pticm_init_states /
+ * pticm_set_states): replicas per block, blocks, threads per block, ICM teams
+ * per block (1: the whole block is one team), whether one block holds one
+ * replica (block team) on the narrow-bound kernel, whether the adjacency is
+ * staged into shared memory, and where the replicas live (0 shared memory,
+ * 1 spins in shared memory with fields gathered at each visit, 2 device
+ * memory).  No counterpart in the reference (one replica per MPI rank). */
+typedef struct pticm_layout {
+    uint32_t replicas_per_block, blocks, threads, icm_teams;
+    int32_t block_team, narrow, adjacency_staged, state_mode;
+} pticm_layout;
+PTICM_API int pticm_get_layout(pticm_ctx* c, pticm_layout* out);
 
 /* Ladder and slot -> replica map (beta_indices of src/replica_exchange.cc). */
 PTICM_API int pticm_get_ladder(pticm_ctx* c, double* beta, uint32_t* slot_to_replica, uint32_t* nc);
@@ -265,6 +305,68 @@ typedef struct pticm_trace {
 
 PTICM_API int pticm_replay(pticm_ctx* c, const pticm_trace* t);
 
+/* ------------------------------------------------------ single replicas -- */
+/* One replica in device memory, for code written in the reference's
+ * per-replica shape (its solve loop, src/solver.cc:67-127, and get_beta's
+ * pilot loop, src/cae_estimator.cc:112-140): int8 spins and int32 local
+ * fields, the energy, the best energy and state, flip and sweep counters,
+ * and the FP64 table exp(-beta dE) of its temperature (built on the host
+ * with the reference's expression).  The bulk path (pticm_run) keeps its
+ * replicas in a context instead. */
+typedef struct pticm_replica pticm_replica;
+typedef struct pticm_replica_info {
+    double energy, beta, best_energy;   /* best_energy: DBL_MAX before the first accepted flip */
+    uint64_t best_sweep, flips, sweeps;
+} pticm_replica_info;
+
+/* Replica(Problem&, beta, init_state, init_dE, energy) include/replica.hh:27-33,
+ * src/replica.cc:40-60: n bytes of 0/1 spins; the local fields and the energy
+ * are computed from them (calculate_dE); best energy "none yet". */
+PTICM_API int pticm_replica_create(const pticm_problem* p, double beta, const uint8_t* state, pticm_replica** out);
+/* Replica::operator= (include/replica.hh:54-67): a new replica with the same
+ * spins, fields, energies, counters and temperature. */
+PTICM_API int pticm_replica_copy(const pticm_replica* src, pticm_replica** out);
+PTICM_API void pticm_replica_destroy(pticm_replica* r);
+/* Replica::set_beta (include/replica.hh:44). */
+PTICM_API int pticm_replica_set_beta(pticm_replica* r, double beta);
+/* Replica::set_state with the fields and energy recomputed from it. */
+PTICM_API int pticm_replica_set_state(pticm_replica* r, const uint8_t* state);
+/* Replica::set_energy / set_ene (include/replica.hh:36,43): an integer energy. */
+PTICM_API int pticm_replica_set_energy(pticm_replica* r, double energy);
+/* Replica(..., log_ene, burn_in): log the energy after every site visit of
+ * the sweeps after the first burn_in (src/replica.cc:10-12). */
+PTICM_API int pticm_replica_set_logging(pticm_replica* r, int log_energy, uint64_t burn_in);
+/* Replica::sweep (src/replica.cc:5-38) on the GPU: sites 0..n-1 in order, a
+ * move with dE <= 0 accepted, else accepted iff the next uniform is below
+ * exp(-beta dE); fields, energy, flips and best state as mh_accept.  The
+ * uniforms are the caller's (Problem::rand_double draws, src/replica.cc:36);
+ * pass n_uniforms >= the sites (one per site at most); *consumed receives how
+ * many the sweep used, so that the caller's generator can be advanced by
+ * exactly that many.  *energy (may be NULL) receives the energy after the
+ * sweep; energy_log (n values, may be NULL) the energy after every site when
+ * logging is on and the sweep is past the burn-in. */
+PTICM_API int pticm_replica_sweep(pticm_replica* r, const double* uniforms, uint64_t n_uniforms, uint64_t* consumed,
+                                  double* energy, double* energy_log);
+/* Replica's getters (include/replica.hh:35-50): info, the state (n bytes),
+ * dE_i = -2 s_i (h_i + f_i) (n doubles) and the best state; any may be NULL. */
+PTICM_API int pticm_replica_get(pticm_replica* r, pticm_replica_info* info, uint8_t* state, double* dE,
+                                uint8_t* best_state);
+
+/* xor_icm (src/icm.cc:8-35) on two states of n 0/1 bytes, without its seed
+ * draw, on the GPU: s1 is negated when more than n/2 sites differ; *count
+ * receives the number of differing sites and `sites` (n entries, may be
+ * NULL) their indices ascending -- the population std::sample draws the seed
+ * from (src/icm.cc:33). */
+PTICM_API int pticm_problem_icm_overlap(const pticm_problem* p, uint8_t* s1, const uint8_t* s2, uint64_t* count,
+                                        int64_t* sites);
+/* bfs_icm (src/icm.cc:37-72) on the GPU: the seed's connected set of sites
+ * where s1 and s2 differ is flipped in both. */
+PTICM_API int pticm_problem_icm_cluster(const pticm_problem* p, int64_t seed, uint8_t* s1, uint8_t* s2);
+/* Problem::incremental_dE (src/problem.cc:164-181) on the GPU: dE (n
+ * doubles) after site `index` of `state` (its value before the flip) flips. */
+PTICM_API int pticm_problem_incremental_dE(const pticm_problem* p, double* dE, const uint8_t* state,
+                                           uint32_t index);
+
 /* ----------------------------------------------- no device allocation -- */
 /* For callers that cannot call cudaMalloc (their host framework owns every
  * device allocation and hands out buffers, or they must avoid the implicit
@@ -304,12 +406,14 @@ PTICM_API int pticm_run_noalloc(const pticm_problem* p, const pticm_opts* o, con
                       const pticm_noalloc_io* io, uint64_t step0, uint64_t pt_steps, void* stream);
 
 /* --------------------------------------------------- tensor-core GEMM -- */
-/* C[M x N] = act(A[M x K] . B[N x K]^T + bias) on the tcgen05 tensor cores
- * (BF16 operands given as raw uint16 bit patterns, K-major; FP32 result;
- * act 0 = none, 1 = SiLU; K a multiple of 64).  Host buffers; used to check
- * the surrogate network's GEMM against a reference. */
+/* A[M x K] . B[N x K]^T + bias on the tcgen05 tensor cores (BF16 operands
+ * given as raw uint16 bit patterns, K-major; FP32 accumulation; K a multiple
+ * of 64), with the epilogue of the surrogate network's layers: C receives the
+ * FP32 result before the activation, C_bf16 (may be NULL) the BF16 output
+ * after it (act 0 = none, 1 = SiLU), as the hidden layers store it.  Host
+ * buffers; used to check the network's GEMM against a reference. */
 PTICM_API int pticm_tc_gemm_check(int M, int N, int K, const uint16_t* A, const uint16_t* B, const float* bias,
-                                  int act, float* C);
+                                  int act, float* C, uint16_t* C_bf16);
 /* Device time of the tensor-core GEMM at M x N x K (bf16 operands and
  * output, FP32 accumulation), averaged over `iters` back-to-back launches
  * after one warm-up; tflops = 2 M N K / time. */

@@ -7,12 +7,23 @@
 # repository.  -DWHOLE drops the second main() in src/cae_estimator.cc:431-450,
 # -DNDEBUG matches the reference's Release build (CMakeLists.txt:4-8), and the
 # single-rank <mpi.h> stand-in lives in oracle/ref_stub/.  The output directory
-# is git-ignored.  Usage: oracle/build_ref.sh [REFERENCE_DIR]
+# is git-ignored.
+#
+#   oracle/build_ref.sh [REFERENCE_DIR | --if-present]
+#
+# The reference directory is the argument, else $PTICM_REFERENCE_DIR, else
+# the read-only checkout this recipe was written against.  With --if-present
+# a missing checkout is not an error (machines without the reference, such as
+# the GPU hosts, use the C oracle alone).
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${1:-${PTICM_REFERENCE_DIR:-/root/reference}}"
+OPTIONAL=0
+ARG="${1:-}"
+if [ "$ARG" = "--if-present" ]; then OPTIONAL=1; ARG=""; fi
+REF="${ARG:-${PTICM_REFERENCE_DIR:-/root/reference}}"
 OUT="$HERE/_ref"
 if [ ! -d "$REF/src" ]; then
+    if [ "$OPTIONAL" = 1 ]; then exit 0; fi
     echo "reference sources not found at $REF" >&2
     exit 2
 fi

@@ -518,12 +518,18 @@ struct orc_trace {
     vec_t icm;      /* int64   : ICM seed site, -1 when the pair is equal    */
     vec_t init;     /* uint8   : initial states, replica-major               */
     vec_t energy;   /* double  : slot energies after the sweeps of each step */
+    int energy_only;/* record the slot energies alone (long runs)            */
 };
 
 orc_trace* orc_trace_new(void) {
     orc_trace* t = (orc_trace*)calloc(1, sizeof(orc_trace));
     t->u.el = sizeof(double); t->off.el = sizeof(uint64_t); t->xk.el = sizeof(int32_t);
     t->xlu.el = sizeof(double); t->icm.el = sizeof(int64_t); t->init.el = 1; t->energy.el = sizeof(double);
+    return t;
+}
+orc_trace* orc_trace_new_energy_only(void) {
+    orc_trace* t = orc_trace_new();
+    t->energy_only = 1;
     return t;
 }
 void orc_trace_free(orc_trace* t) {
@@ -657,6 +663,31 @@ static void bfs_icm(const orc_problem* p, int64_t seed, uint8_t* s1, uint8_t* s2
     }
 }
 
+/* xor_icm's overlap (src/icm.cc:8-31) without the seed draw: s1 is negated
+ * when more than N/2 sites differ, as there; the differing sites, ascending,
+ * go to `sites`; returns their count. */
+int64_t orc_overlap(const orc_problem* p, uint8_t* s1, const uint8_t* s2, int64_t* sites) {
+    uint64_t N = (uint64_t)p->n, cnt = 0;
+    for (uint64_t j = 0; j < N; j++) if (s1[j] ^ s2[j]) sites[cnt++] = (int64_t)j;
+    if (cnt > N / 2) {
+        cnt = 0;
+        for (uint64_t j = 0; j < N; j++) {
+            s1[j] = !s1[j];
+            if (s1[j] != s2[j]) sites[cnt++] = (int64_t)j;
+        }
+    }
+    return (int64_t)cnt;
+}
+
+/* bfs_icm (src/icm.cc:37-72) on caller states from a caller seed. */
+void orc_bfs_icm(const orc_problem* p, int64_t seed, uint8_t* s1, uint8_t* s2) {
+    int64_t* stack = (int64_t*)malloc(((size_t)p->n + 1) * sizeof(int64_t));
+    uint8_t* added = (uint8_t*)malloc((size_t)p->n + 1);
+    bfs_icm(p, seed, s1, s2, stack, added);
+    free(stack);
+    free(added);
+}
+
 /* icm (src/icm.cc:74-215), both replicas on rank 0. */
 static int icm_step(pt_t* w, uint64_t target, uint8_t* t1, uint8_t* t2, int64_t* tmp, uint8_t* added) {
     uint64_t N = w->N;
@@ -686,6 +717,10 @@ int orc_solve(orc_problem* p, const orc_params* prm, orc_result* res,
     memset(&W, 0, sizeof(W));
     pt_t* w = &W;
     w->p = p;
+    /* the decision trace (uniforms, exchanges, seeds) unless only the slot
+     * energies are wanted */
+    orc_trace* energy_tr = trace;
+    if (trace && trace->energy_only) trace = NULL;
     w->tr = trace;
     w->N = (uint64_t)p->n;
     uint64_t Nt0 = prm->Nt;
@@ -773,7 +808,7 @@ int orc_solve(orc_problem* p, const orc_params* prm, orc_result* res,
                 if (trace) { trace->u.n += used; uint64_t o = trace->u.n; vpush(&trace->off, &o); }
             }
         }
-        if (trace) for (uint64_t k = 0; k < R; k++) vpush(&trace->energy, &w->Eg[w->bidx[k]]);
+        if (energy_tr) for (uint64_t k = 0; k < R; k++) vpush(&energy_tr->energy, &w->Eg[w->bidx[k]]);
         for (uint64_t m = 0; m + 1 < Nt; m++) { try_exchange(w, 0); try_exchange(w, 1); }
         if (prm->icm) {
             for (int64_t k = (int64_t)Nt - 1; k >= (int64_t)Nt - (int64_t)Nc; k--)

@@ -87,7 +87,7 @@ uint64_t orc_sweep_stream(const orc_problem* p, double beta, uint8_t* s, double*
                           const double* u, uint64_t n_u, uint64_t* pos);
 
 /* ------------------------------------------------------------- Ladder ---- */
-void orc_beta_linspace(double* beta, double T0, double T1, uint64_t nt, int inverse); /* src/mpi_utils.cc:6-22 */
+void orc_beta_linspace(double* beta, double T0, double T1, uint64_t nt, int inverse); /* src/utils.cc:6-22 */
 
 /* ------------------------------------------------------------ Solver ----- */
 typedef struct orc_params {
@@ -122,6 +122,9 @@ typedef struct orc_result {
 /* Optional trace of every random decision, for the device replay. */
 typedef struct orc_trace orc_trace;
 orc_trace* orc_trace_new(void);
+/* A trace that records only the slot energies after the sweeps of each step
+ * (no uniforms or decisions): statistics of long runs. */
+orc_trace* orc_trace_new_energy_only(void);
 void orc_trace_free(orc_trace* t);
 /* accessors (sizes first, then copies into caller buffers) */
 uint64_t orc_trace_n_uniforms(const orc_trace* t);
@@ -140,6 +143,15 @@ void orc_trace_copy(const orc_trace* t, double* uniforms, uint64_t* sweep_offset
 int orc_solve(orc_problem* p, const orc_params* prm, orc_result* res,
               uint8_t* best_state, uint8_t* replica_states, double* final_energy,
               orc_trace* trace);
+
+/* ------------------------------------------------------- One ICM pair ---- */
+/* xor_icm's overlap (src/icm.cc:8-31) without its seed draw: negates s1 when
+ * more than N/2 sites differ; writes the differing sites ascending to
+ * `sites` (N entries) and returns their count. */
+int64_t orc_overlap(const orc_problem* p, uint8_t* s1, const uint8_t* s2, int64_t* sites);
+/* bfs_icm (src/icm.cc:37-72): flips the seed's cluster of differing sites in
+ * both states. */
+void orc_bfs_icm(const orc_problem* p, int64_t seed, uint8_t* s1, uint8_t* s2);
 
 /* ---------------------------------------------- Multihistogram (CAE) ----- */
 /* Restatements of src/cae_estimator.cc: the pilot run (gather_samples :76-151),

@@ -89,6 +89,10 @@ def lib():
         L.orc_sweep.restype = C.c_uint64
         L.orc_beta_linspace.argtypes = [P, C.c_double, C.c_double, C.c_uint64, C.c_int]
         L.orc_trace_new.restype = P
+        L.orc_trace_new_energy_only.restype = P
+        L.orc_overlap.argtypes = [P, P, P, P]
+        L.orc_overlap.restype = C.c_int64
+        L.orc_bfs_icm.argtypes = [P, C.c_int64, P, P]
         L.orc_trace_free.argtypes = [P]
         for f in ("orc_trace_n_uniforms", "orc_trace_n_sweeps", "orc_trace_n_exchange",
                   "orc_trace_n_icm", "orc_trace_n_init", "orc_trace_n_energy"):
@@ -223,10 +227,32 @@ def sweep_stream(prob: Problem, beta, s, uniforms, n_sweeps=1):
                 best_state=best, flips=flips, consumed=pos.value, energies=energies)
 
 
+def overlap(prob: Problem, s1, s2):
+    """xor_icm's overlap (src/icm.cc:8-31) without the seed draw: returns s1
+    (negated when more than N/2 sites differ) and the differing sites."""
+    a = np.array(s1, dtype=np.uint8)
+    b = np.ascontiguousarray(s2, dtype=np.uint8)
+    sites = np.zeros(max(prob.n, 1), np.int64)
+    cnt = lib().orc_overlap(prob.h, _p(a), _p(b), _p(sites))
+    return a, sites[:cnt]
+
+
+def bfs_icm(prob: Problem, seed, s1, s2):
+    """bfs_icm (src/icm.cc:37-72): both states with the seed's cluster of
+    differing sites flipped."""
+    a = np.array(s1, dtype=np.uint8)
+    b = np.array(s2, dtype=np.uint8)
+    lib().orc_bfs_icm(prob.h, int(seed), _p(a), _p(b))
+    return a, b
+
+
 def solve(prob: Problem, *, seed, Nt, pts, sweeps=1, T0=0.6, T1=2.8, inverse=False, icm=False,
-          preprocess=False, pre_samples=2000, pre_step=0.1, pilot_burn_in=5000, trace=False):
+          preprocess=False, pre_samples=2000, pre_step=0.1, pilot_burn_in=5000, trace=False,
+          energies=False):
     """`pticm::solve` on one rank (src/solver.cc:16-166).  The problem's engine
-    is re-seeded with `seed` first, as src/problem.cc:183 does."""
+    is re-seeded with `seed` first, as src/problem.cc:183 does.  trace=True
+    records every random decision; energies=True records only the slot
+    energies after the sweeps of each step (out["step_energy"], [pts, 2 Nt])."""
     L = lib()
     L.orc_mt64_seed(prob.rng(), seed)
     prm = Params(seed, Nt, pts, sweeps, pre_samples, pilot_burn_in, T0, T1, pre_step,
@@ -236,7 +262,7 @@ def solve(prob: Problem, *, seed, Nt, pts, sweeps=1, T0=0.6, T1=2.8, inverse=Fal
     best = np.zeros(n, np.uint8)
     states = np.zeros(2 * Nt * n, np.uint8)
     fe = np.zeros(2 * Nt, np.float64)
-    tr = L.orc_trace_new() if trace else None
+    tr = L.orc_trace_new() if trace else (L.orc_trace_new_energy_only() if energies else None)
     rc = L.orc_solve(prob.h, C.byref(prm), C.byref(res), _p(best), _p(states), _p(fe), tr)
     if rc:
         if tr:
@@ -251,7 +277,13 @@ def solve(prob: Problem, *, seed, Nt, pts, sweeps=1, T0=0.6, T1=2.8, inverse=Fal
                best_state_energy=res.best_state_energy, best_maxcut=res.best_maxcut,
                flips=res.flips, flips_u64=res.flips_u64, best_state=best,
                states=states[: R * n].reshape(R, n), final_energy=fe[:R], char_scale=res.char_scale)
-    if tr:
+    if tr and not trace:
+        ne = L.orc_trace_n_energy(tr)
+        se = np.zeros(max(ne, 1))
+        L.orc_trace_copy(tr, None, None, None, None, None, None, _p(se))
+        L.orc_trace_free(tr)
+        out["step_energy"] = se[:ne].reshape(-1, R) if ne else np.zeros((0, R))
+    elif tr:
         nu = L.orc_trace_n_uniforms(tr)
         ns = L.orc_trace_n_sweeps(tr)
         nx = L.orc_trace_n_exchange(tr)

@@ -38,7 +38,7 @@ int mlp_fail(int code, const std::string& m) {
 }  // namespace
 
 extern "C" int pticm_tc_gemm_check(int M, int N, int K, const uint16_t* A, const uint16_t* B, const float* bias,
-                                   int act, float* C) {
+                                   int act, float* C, uint16_t* C_bf16) {
     if (M <= 0 || N <= 0 || K <= 0 || (K % 64) || !A || !B || !C)
         return mlp_fail(PTICM_ERR_INVALID, "need positive M, N and K a multiple of 64");
     int count = 0;
@@ -46,15 +46,16 @@ extern "C" int pticm_tc_gemm_check(int M, int N, int K, const uint16_t* A, const
         return mlp_fail(PTICM_ERR_NODEVICE, "no CUDA device is available");
     __nv_bfloat16 *dA = nullptr, *dB = nullptr;
     float *dC = nullptr, *db = nullptr;
+    __nv_bfloat16* dCb = nullptr;
     DevStatus* ds = nullptr;
     int* dab = nullptr;
     int rc = PTICM_OK;
     auto cleanup = [&]() {
-        cudaFree(dA); cudaFree(dB); cudaFree(dC); cudaFree(db); cudaFree(ds); cudaFree(dab);
+        cudaFree(dA); cudaFree(dB); cudaFree(dC); cudaFree(dCb); cudaFree(db); cudaFree(ds); cudaFree(dab);
     };
     if (cudaMalloc(&dA, (size_t)M * K * 2) || cudaMalloc(&dB, (size_t)N * K * 2) ||
         cudaMalloc(&dC, (size_t)M * N * 4) || cudaMalloc(&ds, sizeof(DevStatus)) || cudaMalloc(&dab, 4) ||
-        (bias && cudaMalloc(&db, (size_t)N * 4))) {
+        (bias && cudaMalloc(&db, (size_t)N * 4)) || (C_bf16 && cudaMalloc(&dCb, (size_t)M * N * 2))) {
         cleanup();
         return mlp_fail(PTICM_ERR_NOMEM, "device allocation failed");
     }
@@ -63,11 +64,12 @@ extern "C" int pticm_tc_gemm_check(int M, int N, int K, const uint16_t* A, const
     if (e == cudaSuccess && bias) e = cudaMemcpy(db, bias, (size_t)N * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(ds, 0, sizeof(DevStatus));
     if (e == cudaSuccess) e = cudaMemset(dab, 0, 4);
-    if (e == cudaSuccess) e = tc_gemm(dA, dB, M, N, K, db, act, dC, nullptr, N, ds, dab, nullptr);
+    if (e == cudaSuccess) e = tc_gemm(dA, dB, M, N, K, db, act, dC, dCb, N, ds, dab, nullptr);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     DevStatus hs{};
     if (e == cudaSuccess) e = cudaMemcpy(&hs, ds, sizeof hs, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(C, dC, (size_t)M * N * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && C_bf16) e = cudaMemcpy(C_bf16, dCb, (size_t)M * N * 2, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) rc = mlp_fail(PTICM_ERR_CUDA, std::string("tc_gemm: ") + cudaGetErrorString(e));
     else if (hs.error) rc = mlp_fail(PTICM_ERR_DEVICE, "tc_gemm: tensor-core wait expired");
     cleanup();

@@ -20,12 +20,14 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <string>
 #include <vector>
 
 #include "pticm.h"
+#include "pticm_device.cuh"
 #include "pticm_engine.h"
 #include "problem_host.h"
 #include "runtime_internal.h"
@@ -81,6 +83,32 @@ __global__ void export_spins(const int8_t* spins, uint8_t* out, const int32_t* p
     }
 }
 
+// The caller's slot map and pair order are used as indices by the engine:
+// check that each is a permutation (slot: of 0..R-1, order: of 0..nt-2)
+// before it runs.  `seen` holds R + nt - 1 zeroed counters; a value out of
+// range or seen twice records DEV_BAD_INDEX in the status word.
+__global__ void check_perms(const uint32_t* slot, int R, const uint32_t* order, int m, unsigned* seen,
+                            DevStatus* st) {
+    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < R + m; x += gridDim.x * blockDim.x) {
+        const bool is_slot = x < R;
+        const uint32_t v = is_slot ? slot[x] : order[x - R];
+        const uint32_t lim = is_slot ? (uint32_t)R : (uint32_t)m;
+        bool bad = v >= lim;
+        if (!bad) bad = atomicAdd(seen + (is_slot ? 0 : R) + v, 1u) != 0u;
+        if (bad && atomicCAS(&st->error, 0, (int)DEV_BAD_INDEX) == 0) {
+            st->where = is_slot ? 1 : 2;
+            st->aux0 = is_slot ? x : x - R;
+            st->aux1 = v;
+        }
+    }
+}
+
+// Every best energy starts at "none yet" (the largest int64, as elsewhere in
+// the library).
+__global__ void fill_no_best(long long* bestE, int R) {
+    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < R; x += gridDim.x * blockDim.x) bestE[x] = kNoBest;
+}
+
 // Bump allocator over the scratch array (256-byte aligned regions).
 struct Carve {
     size_t off = 0;
@@ -105,6 +133,8 @@ extern "C" int pticm_run_noalloc(const pticm_problem* p, const pticm_opts* o, co
     if (o->chains < 1 || o->chains > 16 || (o->icm && (o->chains % 2)))
         return noalloc_fail(PTICM_ERR_INVALID, "chains must be in [1, 16] (even with ICM)");
     if (o->sweeps < 1 || o->exchange > 1 || o->icm_algo > 3) return noalloc_fail(PTICM_ERR_INVALID, "invalid options");
+    for (uint32_t k = 0; k < nt; k++)
+        if (!std::isfinite(beta[k])) return noalloc_fail(PTICM_ERR_INVALID, "non-finite inverse temperature");
     const HostProblem& P = problem_host(p);
     const int R = (int)(nt * o->chains);
     InstanceDesc D{};
@@ -141,6 +171,7 @@ extern "C" int pticm_run_noalloc(const pticm_problem* p, const pticm_opts* o, co
     const size_t o_flips = cv.take(RR * 8), o_bestE = cv.take(RR * 8), o_bestS = cv.take(RR * 8);
     const size_t o_bstate = cv.take(RR * npad), o_slot = cv.take(RR * 4), o_order = cv.take((size_t)nt * 4);
     const size_t o_att = cv.take(RR * 8), o_succ = cv.take(RR * 8);
+    const size_t o_seen = cv.take((RR + nt) * 4);
     if (cv.off > (size_t)PTICM_NOALLOC_SCRATCH_BYTES)
         return noalloc_fail(PTICM_ERR_UNSUPPORTED,
                             "run needs " + std::to_string(cv.off) + " bytes of working memory; pticm_run_noalloc is limited to " +
@@ -173,7 +204,6 @@ extern "C" int pticm_run_noalloc(const pticm_problem* p, const pticm_opts* o, co
     NA_CK(cudaMemsetAsync(base + o_bar, 0, 2 * sizeof(unsigned), st));
     NA_CK(cudaMemsetAsync(base + o_flips, 0, RR * 8, st));
     NA_CK(cudaMemsetAsync(base + o_bestS, 0, RR * 8, st));
-    NA_CK(cudaMemsetAsync(base + o_bestE, 0x7F, RR * 8, st));   // "no best yet": 0x7F7F...7F
     NA_CK(cudaMemsetAsync(base + o_att, 0, RR * 8, st));
     NA_CK(cudaMemsetAsync(base + o_succ, 0, RR * 8, st));
     if (io->slot_to_replica)
@@ -184,6 +214,26 @@ extern "C" int pticm_run_noalloc(const pticm_problem* p, const pticm_opts* o, co
         NA_CK(cudaMemcpyAsync(base + o_order, io->pair_order, (size_t)(nt - 1) * 4, cudaMemcpyDeviceToDevice, st));
     else
         NA_CK(cudaMemcpyAsync(base + o_order, order0.data(), (size_t)nt * 4, cudaMemcpyHostToDevice, st));
+    // the slot map and pair order must be permutations before the engine
+    // indexes with them (also those passed in by the caller)
+    NA_CK(cudaMemsetAsync(base + o_seen, 0, (RR + nt) * 4, st));
+    check_perms<<<std::max(1, std::min(64, (int)((RR + nt + 255) / 256))), 256, 0, st>>>(
+        reinterpret_cast<const uint32_t*>(base + o_slot), R, reinterpret_cast<const uint32_t*>(base + o_order),
+        (int)nt - 1, reinterpret_cast<unsigned*>(base + o_seen), reinterpret_cast<DevStatus*>(base + o_status));
+    NA_CK(cudaGetLastError());
+    {
+        DevStatus cs{};
+        NA_CK(cudaMemcpyAsync(&cs, base + o_status, sizeof(cs), cudaMemcpyDeviceToHost, st));
+        NA_CK(cudaStreamSynchronize(st));
+        if (cs.error)
+            return noalloc_fail(PTICM_ERR_INVALID,
+                                std::string(cs.where == 1 ? "slot_to_replica is not a permutation of 0..R-1"
+                                                          : "pair_order is not a permutation of 0..nt-2") +
+                                    " (entry " + std::to_string(cs.aux0) + " = " + std::to_string(cs.aux1) + ")");
+    }
+    fill_no_best<<<std::max(1, std::min(64, (R + 255) / 256)), 256, 0, st>>>(
+        reinterpret_cast<long long*>(base + o_bestE), R);
+    NA_CK(cudaGetLastError());
 
     EngineArgs A{};
     A.desc = reinterpret_cast<const InstanceDesc*>(base + o_desc);

@@ -237,6 +237,18 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
     uint8_t* d = X.d;
     const int nwords = (n + 31) >> 5;
     if (threadIdx.x == 0) P.subtick(PROF_ICM_ENERGY);
+    // a caller's seed for this pair (device numbering), or skip the pair
+    int forced = -1;
+    const bool exact = REPLAY || A.icm_exact != 0;
+    if (!REPLAY && A.icm_force != nullptr) {
+        const long long f = A.icm_force[q];
+        if (f == -2) return 0;
+        if (f >= (long long)n || f < -2) {
+            if (team.tr == 0) dev_fail(A.status, A.abort_flag, DEV_BAD_INDEX, where_err + 5, q, f);
+            return 0;
+        }
+        if (f >= 0) forced = A.perm[D.perm_off + f];
+    }
 
     // overlap, its size, seed candidates among differing and equal sites
     unsigned long long r64 = 0;
@@ -305,6 +317,14 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
         for (int w = team.tr; w < nwords; w += team.ts) X.vis[w] = 0u;
     team.reduce(cnt, kd, ke, hs);
     const bool gflip = cnt > (long long)(n / 2);
+    if (forced >= 0 && (d[forced] != 0) == gflip) {
+        // a caller's seed must be a differing site after the global flip:
+        // report it before any state changes (and clear the list counters)
+        if (team.tr == 0) dev_fail(A.status, A.abort_flag, DEV_BAD_INDEX, where_err + 6, q, forced);
+        if (BLOCK && team.tr == 0) { team.ctl[2] = 0; team.ctl[3] = 0; team.ctl[4] = 0; }
+        team.sync();
+        return 0;
+    }
     // the overlap list of a block team: [l0, l0 + llen) of lst
     const int l0 = gflip ? (int)cnt : 0, llen = gflip ? n - (int)cnt : (int)cnt;
     auto for_overlap = [&](auto&& f) {
@@ -346,7 +366,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
             }
         }
     } else if (cnt > 0) {
-        seed = (int)((gflip ? ke : kd) & 0xFFFFFFFFull);
+        seed = forced >= 0 ? forced : (int)((gflip ? ke : kd) & 0xFFFFFFFFull);
         if (seed < 0 || seed >= n) {
             if (team.tr == 0) dev_fail(A.status, A.abort_flag, DEV_BAD_INDEX, where_err + 4, q, seed);
             return 0;
@@ -546,7 +566,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                     long long none = 0;
                     team.reduce(c, m1, m2, none);
                     csize = (rs == rL) ? cnt - c : c;
-                    const bool sw = !REPLAY && csize * 2 > cnt;
+                    const bool sw = !exact && csize * 2 > cnt;
                     fast = (rs == rL) ? sw : !sw;   // the flipped set lies in S
                     fast_root = rs == rL ? rL : rs;
                     fast_eq = rs != rL;
@@ -625,7 +645,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
         // of the two chains' configurations at one temperature, which leaves
         // the joint distribution of the (independent, identical) chains
         // invariant.  Replay keeps the reference's flips.
-        swapped = (!REPLAY && csize * 2 > cnt) ? 1 : 0;
+        swapped = (!exact && csize * 2 > cnt) ? 1 : 0;
         const uint8_t fmark = swapped ? 1 : 2;
         const long long fsize = swapped ? cnt - csize : csize;
         // membership of an overlap site in the flipped set
@@ -1276,7 +1296,7 @@ __global__ void __launch_bounds__((REPLAY || (BLOCKTEAM && !NARROW)) ? 1024 : kN
         }
     }
     if (staged) {
-        if (!mbar_wait_bounded(mbar, bulk_parity) && tid == 0)
+        if (!mbar_wait_bounded(mbar, bulk_parity, A.wait_limit_ns ? A.wait_limit_ns : kWaitLimitNs) && tid == 0)
             dev_fail(A.status, A.abort_flag, DEV_TMA_TIMEOUT, 2, blockIdx.x, inst);
         bulk_parity ^= 1u;
     }
@@ -1333,7 +1353,9 @@ __global__ void __launch_bounds__((REPLAY || (BLOCKTEAM && !NARROW)) ? 1024 : kN
                 const long long base = parity * A.spins_pub_half + D.spin_off + (long long)B.r0 * npad;
                 for (int idx = tid; idx < rpc * npad; idx += T) A.spins_pub[base + idx] = B.spin[idx];
             }
-            if (!group_barrier(A.bar + 2 * inst, (unsigned)D.group, abortf, A.status, bar_gen)) break;
+            if (!group_barrier(A.bar + 2 * inst, (unsigned)(D.group + A.bar_phantom), abortf, A.status, bar_gen,
+                               A.wait_limit_ns ? A.wait_limit_ns : kWaitLimitNs))
+                break;
             for (int r = tid; r < R; r += T)
                 if (r < B.r0 || r >= B.r0 + rpc) B.E[r] = ld_cg(A.energy_pub + parity * A.energy_pub_half + D.rep_off + r);
             __syncthreads();

@@ -38,7 +38,8 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
     return t;
 }
 
-// Waits on other blocks give up after this many nanoseconds.
+// Waits on other blocks give up after this many nanoseconds (the default of
+// EngineArgs::wait_limit_ns).
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;
 
 // --------------------------------------------------------------------- RNG
@@ -197,11 +198,13 @@ __device__ __forceinline__ void red_add_release_gpu(unsigned int* p, unsigned in
 // the others poll with acquire loads.  `gen` is thread 0's copy of the
 // generation (read when the block joins the group; the generation cannot
 // move before every block has arrived), so arriving costs one atomic.
-// Waits are bounded: after kWaitLimitNs, or when another block has raised
+// Waits are bounded: after `limit_ns`, or when another block has raised
 // `abort`, the barrier records the failure and returns false.  Callers
-// return when it fails.
+// return when it fails.  `nblocks` may exceed the blocks that arrive (a
+// test hook counts arrivals that never come, so that every wait runs out).
 __device__ __forceinline__ bool group_barrier(unsigned int* bar, unsigned int nblocks, volatile int* abort_flag,
-                                              DevStatus* st, unsigned int& gen) {
+                                              DevStatus* st, unsigned int& gen,
+                                              unsigned long long limit_ns = kWaitLimitNs) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -216,7 +219,7 @@ __device__ __forceinline__ bool group_barrier(unsigned int* bar, unsigned int nb
             unsigned int spins = 0;
             while (ld_acquire_gpu(bar + 1) == g) {
                 if (*abort_flag) { ok = 0; break; }
-                if ((++spins & 63u) == 0 && globaltimer_ns() - t0 > kWaitLimitNs) {
+                if ((++spins & 63u) == 0 && globaltimer_ns() - t0 > limit_ns) {
                     dev_fail(st, abort_flag, DEV_BARRIER_TIMEOUT, 1, blockIdx.x, g);
                     ok = 0;
                     break;
@@ -269,11 +272,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // Bounded wait for phase `parity` of an mbarrier; false on timeout.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                  unsigned long long limit_ns = kWaitLimitNs) {
     const unsigned long long t0 = globaltimer_ns();
     unsigned int spins = 0;
     while (!mbar_try_wait(bar, parity)) {
-        if ((++spins & 255u) == 0 && globaltimer_ns() - t0 > kWaitLimitNs) return false;
+        if ((++spins & 255u) == 0 && globaltimer_ns() - t0 > limit_ns) return false;
     }
     return true;
 }

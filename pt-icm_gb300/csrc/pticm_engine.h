@@ -151,6 +151,17 @@ struct EngineArgs {
     long long* mag_pub;
     SmemPlan sm;
     ReplayArgs replay;
+    // optional ICM controls: per pair q a seed site in the original numbering
+    // (-1: the random choice, -2: skip the pair); icm_exact flips the seed's
+    // cluster itself, never the rest of the overlap
+    const long long* icm_force;
+    int32_t icm_exact;
+    // bounded waits: the limit of every wait on other blocks or on bulk
+    // copies (0: kWaitLimitNs), and arrivals a group barrier counts beyond
+    // the group's blocks (0 in production; a test hook that makes the
+    // barrier's wait run out)
+    int32_t bar_phantom;
+    unsigned long long wait_limit_ns;
 };
 
 enum EngineFlags : int32_t {

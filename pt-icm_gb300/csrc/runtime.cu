@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "pticm.h"
+#include "pticm_device.cuh"
 #include "pticm_engine.h"
 #include "problem_host.h"
 #include "runtime_internal.h"
@@ -65,8 +66,8 @@ int check_device() {
 
 struct pticm_problem {
     HostProblem hp;
-    // device copy for pticm_problem_evaluate
-    DArr<int32_t> d_row, d_h;
+    // device copy for pticm_problem_evaluate and the single-replica calls
+    DArr<int32_t> d_row, d_h, d_perm, d_iperm;
     DArr<uint32_t> d_adj;
     bool uploaded = false;
 };
@@ -105,6 +106,10 @@ struct pticm_ctx {
     DArr<uint8_t> d_states_in;  // caller states in the original site order (pticm_set_states)
     DArr<uint8_t> d_icm_pool;   // ICM scratch when the replicas live in device memory
     long long icm_stride = 0;
+    DArr<long long> d_icm_force;   // per-pair seeds of pticm_icm_pairs
+    // bounded waits: limit (0 = kWaitLimitNs) and the barrier test hook
+    unsigned long long wait_limit_ns = 0;
+    int bar_phantom = 0;
     // the inputs of the last launch configuration (it depends on nothing else
     // once the context exists): replay, ICM pairs, histogram rows
     bool configured = false;
@@ -516,6 +521,8 @@ EngineArgs make_args(pticm_ctx* c) {
     A.flags = engine_flags(c->P, c->o);
     A.icm_pool = c->d_icm_pool.p;
     A.icm_pool_stride = c->icm_stride;
+    A.wait_limit_ns = c->wait_limit_ns;
+    A.bar_phantom = c->bar_phantom;
     return A;
 }
 
@@ -740,6 +747,29 @@ int slot_hist_dos(const unsigned* rows, int nt, int chains, long long nbins, lon
 }
 
 const HostProblem& problem_host(const pticm_problem* p) { return p->hp; }
+
+int problem_device(const pticm_problem* pc, ProblemDevice* out) {
+    pticm_problem* p = const_cast<pticm_problem*>(pc);
+    const HostProblem& P = p->hp;
+    if (!p->uploaded) {
+        CK(p->d_row.upload(P.drow, 4));
+        CK(p->d_adj.upload(P.dadj, 4));
+        CK(p->d_h.upload(P.dh, 4));
+        CK(p->d_perm.upload(P.perm, 4));
+        CK(p->d_iperm.upload(P.iperm, 4));
+        p->uploaded = true;
+    }
+    out->row = p->d_row.p;
+    out->adj = p->d_adj.p;
+    out->h = p->d_h.p;
+    out->perm = p->d_perm.p;
+    out->iperm = p->d_iperm.p;
+    out->n = (int)P.n;
+    out->n_pad = pad16(P.n);
+    out->kmax = P.kmax;
+    out->has_h = P.has_h;
+    return PTICM_OK;
+}
 void set_last_error(const std::string& m) { g_err = m; }
 
 }  // namespace pticm
@@ -814,12 +844,8 @@ int pticm_problem_evaluate(const pticm_problem* pc, int64_t count, const uint8_t
     pticm_problem* p = const_cast<pticm_problem*>(pc);
     const HostProblem& P = p->hp;
     const int n = (int)P.n, npad = pad16(n);
-    if (!p->uploaded) {
-        CK(p->d_row.upload(P.drow, 4));
-        CK(p->d_adj.upload(P.dadj, 4));
-        CK(p->d_h.upload(P.dh, 4));
-        p->uploaded = true;
-    }
+    ProblemDevice PD;
+    if (int rc = problem_device(p, &PD)) return rc;
     std::vector<int8_t> dev((size_t)count * npad, 1);
     for (int64_t g = 0; g < count; g++)
         for (int i = 0; i < n; i++) dev[g * npad + i] = states[g * n + P.perm[i]] ? 1 : -1;
@@ -997,6 +1023,71 @@ int pticm_run(pticm_ctx* c, uint64_t pt_steps, uint32_t phase_mask) {
         if (phase_mask & PHASE_SWEEP) c->attempts += (uint64_t)chunk * c->o.sweeps * (uint64_t)c->R * (uint64_t)c->P.n;
         left -= (uint64_t)chunk;
     }
+    return PTICM_OK;
+}
+
+int pticm_icm_pairs(pticm_ctx* c, const int64_t* seeds, uint32_t count, int exact) {
+    if (!c || !seeds) return fail(PTICM_ERR_INVALID, "null argument");
+    if (!c->ladder_set || !c->states_set) return fail(PTICM_ERR_INVALID, "set the ladder and the states first");
+    const uint32_t pairs = (uint32_t)(c->nc * (c->C / 2));
+    if (count != pairs)
+        return fail(PTICM_ERR_INVALID, "expected one seed per ICM pair (" + std::to_string(pairs) + ")");
+    if (pairs == 0) return PTICM_OK;
+    for (uint32_t q = 0; q < count; q++)
+        if (seeds[q] < -2 || seeds[q] >= c->P.n)
+            return fail(PTICM_ERR_INVALID, "seed " + std::to_string(seeds[q]) + " of pair " + std::to_string(q) +
+                                               " is neither a site, -1 (random) nor -2 (skip)");
+    if (int rc = configure(c, false)) return rc;
+    std::vector<long long> f(seeds, seeds + count);
+    CK(c->d_icm_force.upload(f));
+    if (int rc = reset_flags(c)) return rc;
+    EngineArgs A = make_args(c);
+    A.step0 = c->steps_done;
+    A.nsteps = 1;
+    A.phase_mask = PHASE_ICM;
+    A.icm_force = c->d_icm_force.p;
+    A.icm_exact = exact ? 1 : 0;
+    CK(launch_engine(A, c->threads, false, c->block_team, c->narrow, c->group > 1, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    DevStatus st{};
+    CK(cudaMemcpy(&st, c->d_status.p, sizeof(st), cudaMemcpyDeviceToHost));
+    if (st.error == DEV_BAD_INDEX && st.where == 36)   // ICM site 30 + 6: a seed outside the overlap
+        return fail(PTICM_ERR_INVALID, "the seed of pair " + std::to_string(st.aux0) +
+                                           " is not a site where the pair's states differ");
+    if (int rc = read_status(c, "pticm_icm_pairs")) return rc;
+    c->steps_done += 1;
+    return PTICM_OK;
+}
+
+int pticm_get_layout(pticm_ctx* c, pticm_layout* out) {
+    if (!c || !out) return fail(PTICM_ERR_INVALID, "null argument");
+    if (!c->configured) return fail(PTICM_ERR_INVALID, "the layout is chosen with the first states");
+    out->replicas_per_block = (uint32_t)c->rpc;
+    out->blocks = (uint32_t)c->group;
+    out->threads = (uint32_t)c->threads;
+    out->icm_teams = (uint32_t)c->teams;
+    out->block_team = c->block_team ? 1 : 0;
+    out->narrow = c->narrow ? 1 : 0;
+    out->adjacency_staged = c->plan.stage_adj;
+    out->state_mode = c->plan.state_global ? 2 : (c->plan.field_gather ? 1 : 0);
+    return PTICM_OK;
+}
+
+int pticm_get_exchange_order(pticm_ctx* c, uint32_t* order) {
+    if (!c || !order) return fail(PTICM_ERR_INVALID, "null argument");
+    CK(cudaStreamSynchronize(c->stream));
+    std::vector<uint32_t> o;
+    CK(c->d_order.download(o));
+    for (int k = 0; k + 1 < c->nt; k++) order[k] = o[k];
+    return PTICM_OK;
+}
+
+int pticm_set_wait_limit(pticm_ctx* c, uint64_t limit_ns, uint32_t phantom_arrivals) {
+    if (!c) return fail(PTICM_ERR_INVALID, "null argument");
+    if (limit_ns > 60ull * 1000000000ull) return fail(PTICM_ERR_INVALID, "wait limit above 60 s");
+    if (phantom_arrivals > 1) return fail(PTICM_ERR_INVALID, "phantom_arrivals must be 0 or 1");
+    c->wait_limit_ns = limit_ns;
+    c->bar_phantom = (int)phantom_arrivals;
     return PTICM_OK;
 }
 
@@ -1386,14 +1477,41 @@ int ckpt_dump(CkptFile& F, const DArr<T>& a) {
 }
 
 template <class T>
-int ckpt_restore(CkptFile& F, DArr<T>& a, const char* what) {
+int ckpt_read(CkptFile& F, const DArr<T>& a, const char* what, std::vector<T>& v) {
     const uint64_t bytes = F.get_val<uint64_t>();
     if (!F.ok || bytes != a.n * sizeof(T))
         return fail(PTICM_ERR_INVALID, std::string("checkpoint: ") + what + " does not match the context");
-    std::vector<T> v(a.n);
+    v.assign(a.n, T{});
     F.get(v.data(), bytes);
     if (!F.ok) return fail(PTICM_ERR_IO, std::string("checkpoint: short read in ") + what);
-    if (bytes) CK(cudaMemcpy(a.p, v.data(), bytes, cudaMemcpyHostToDevice));
+    return PTICM_OK;
+}
+
+template <class T>
+int ckpt_restore(CkptFile& F, DArr<T>& a, const char* what) {
+    std::vector<T> v;
+    if (int rc = ckpt_read(F, a, what, v)) return rc;
+    if (!v.empty()) CK(cudaMemcpy(a.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return PTICM_OK;
+}
+
+// The engine indexes with the slot map and the exchange order: a map read
+// from a file must be a permutation (of 0..count-1) before it is uploaded.
+bool is_permutation_of_range(const uint32_t* v, size_t count) {
+    std::vector<char> seen(count, 0);
+    for (size_t i = 0; i < count; i++) {
+        if (v[i] >= count || seen[v[i]]) return false;
+        seen[v[i]] = 1;
+    }
+    return true;
+}
+
+int ckpt_restore_permutation(CkptFile& F, DArr<uint32_t>& a, size_t count, const char* what) {
+    std::vector<uint32_t> v;
+    if (int rc = ckpt_read(F, a, what, v)) return rc;
+    if (count > v.size() || !is_permutation_of_range(v.data(), count))
+        return fail(PTICM_ERR_INVALID, std::string("checkpoint: ") + what + " is not a permutation");
+    if (!v.empty()) CK(cudaMemcpy(a.p, v.data(), v.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     return PTICM_OK;
 }
 
@@ -1483,8 +1601,8 @@ int pticm_checkpoint_load(pticm_ctx* c, const char* path) {
     if (!rc) rc = ckpt_restore(F, c->d_bestSweep, "best sweeps");
     if (!rc) rc = ckpt_restore(F, c->d_att, "swap attempts");
     if (!rc) rc = ckpt_restore(F, c->d_succ, "swap successes");
-    if (!rc) rc = ckpt_restore(F, c->d_slot, "slot map");
-    if (!rc) rc = ckpt_restore(F, c->d_order, "exchange order");
+    if (!rc) rc = ckpt_restore_permutation(F, c->d_slot, (size_t)c->R, "slot map");
+    if (!rc) rc = ckpt_restore_permutation(F, c->d_order, (size_t)std::max(c->nt - 1, 0), "exchange order");
     if (!rc) rc = ckpt_restore(F, c->d_cursor, "exchange cursor");
     if (!rc && hist_nbins > 0) rc = ckpt_restore(F, c->d_hist, "histograms");
     if (!rc && hist_nbins > 0) rc = ckpt_restore(F, c->d_obs, "observables");

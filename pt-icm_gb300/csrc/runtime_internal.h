@@ -114,6 +114,20 @@ int slot_hist_dos(const unsigned* rows, int nt, int chains, long long nbins, lon
 long long energy_bound(const HostProblem& P);
 
 const HostProblem& problem_host(const pticm_problem* p);
+// The device copy of a problem in the engine's site order (uploaded on first
+// use and kept with the problem): CSR rows, packed adjacency (col << 8 |
+// uint8 J), linear terms, perm (device -> original site) and iperm
+// (original -> device site).
+struct ProblemDevice {
+    const int32_t* row;
+    const uint32_t* adj;
+    const int32_t* h;
+    const int32_t* perm;
+    const int32_t* iperm;
+    int n, n_pad, kmax;
+    bool has_h;
+};
+int problem_device(const pticm_problem* p, ProblemDevice* out);
 void set_last_error(const std::string& m);
 
 cudaError_t launch_engine(const EngineArgs& A, int threads, bool replay, bool block_team, bool narrow,

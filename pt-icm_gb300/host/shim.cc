@@ -29,26 +29,29 @@ std::string shortest(double v) {
 }  // namespace
 
 // ------------------------------------------------------------------ Problem
-Problem::Problem(std::string path, uint64_t seed, uint64_t burn_in) : seed_(seed), burn_in_(burn_in) {
+Problem::Problem(std::string path, uint64_t seed, uint64_t burn_in) : seed_(seed), burn_in_(burn_in), rng_(seed) {
     check(pticm_problem_load_gset(path.c_str(), &h_));
     refresh();
 }
 
 Problem::Problem(double* weights, int* src, int* dest, double* linear, uint64_t seed, uint64_t burn_in, uint64_t N,
                  uint64_t M)
-    : seed_(seed), burn_in_(burn_in) {
+    : seed_(seed), burn_in_(burn_in), rng_(seed) {
     std::vector<int32_t> s(src, src + M), d(dest, dest + M);
     check(pticm_problem_from_coo((int64_t)N, (int64_t)M, s.data(), d.data(), weights, linear, &h_));
     refresh();
 }
 
 Problem::Problem(double* formulation, double* linear, uint64_t seed, uint64_t burn_in, uint64_t N)
-    : seed_(seed), burn_in_(burn_in) {
+    : seed_(seed), burn_in_(burn_in), rng_(seed) {
     check(pticm_problem_from_dense((int64_t)N, formulation, linear, &h_));
     refresh();
 }
 
-Problem::Problem(Problem&& o) noexcept : h_(o.h_), info_(o.info_), seed_(o.seed_), burn_in_(o.burn_in_) { o.h_ = nullptr; }
+Problem::Problem(Problem&& o) noexcept
+    : h_(o.h_), info_(o.info_), seed_(o.seed_), burn_in_(o.burn_in_), rng_(o.rng_), unif_(o.unif_) {
+    o.h_ = nullptr;
+}
 
 Problem& Problem::operator=(Problem&& o) noexcept {
     if (this != &o) {
@@ -57,6 +60,8 @@ Problem& Problem::operator=(Problem&& o) noexcept {
         info_ = o.info_;
         seed_ = o.seed_;
         burn_in_ = o.burn_in_;
+        rng_ = o.rng_;
+        unif_ = o.unif_;
         o.h_ = nullptr;
     }
     return *this;
@@ -73,6 +78,14 @@ double Problem::energy(const StateVector& s) const {
     double E = 0, cut = 0;
     check(pticm_problem_evaluate(h_, 1, b.data(), &E, &cut, nullptr));
     return E;
+}
+
+double Problem::energy(bool* s) const { return energy(StateVector(s, s + vcount())); }
+
+void Problem::incremental_dE(std::vector<double>& dE, const StateVector& s, uint32_t index) const {
+    auto b = to_bytes(s);
+    dE.resize(s.size());
+    check(pticm_problem_incremental_dE(h_, dE.data(), b.data(), index));
 }
 
 double Problem::maxcut(const StateVector& s) const {
@@ -161,25 +174,51 @@ void initialize_temperatures(PTWorker& w) {
     w.ctx = nullptr;
     check(pticm_create(w.p.handle(), &o, &w.ctx));
     check(pticm_set_ladder(w.ctx, w.beta_values.data(), (uint32_t)w.params.Nt, -1));
-    uint32_t nc = 0;
-    check(pticm_get_ladder(w.ctx, nullptr, nullptr, &nc));
-    w.Nc = nc;
+    // src/initialization.cc:158-164: the pairs counted from the top slot down
+    // while beta >= the characteristic scale, whether or not ICM is on
+    w.Nc = 0;
+    for (int64_t i = (int64_t)w.params.Nt - 1; i >= 0; i--) {
+        if (w.beta_values[(size_t)i] < w.characteristic_scale) break;
+        w.Nc++;
+    }
     const size_t R = (size_t)w.params.Nt * w.params.chains;
     std::vector<double> doubled;
     for (uint32_t c = 0; c < w.params.chains; c++) doubled.insert(doubled.end(), w.beta_values.begin(), w.beta_values.end());
     w.beta_values = doubled;
     w.beta_indices.assign(R, 0);
+    for (size_t k = 0; k < R; k++) w.beta_indices[k] = (uint32_t)k;
     w.swap_attempts.assign(R, 0);
     w.swap_successes.assign(R, 0);
+    // one worker holds every replica: replica i is in chain i / Nt at slot i
+    // (src/initialization.cc:120-172 with numw = 1)
+    w.worker_r = w.last_r = w.loc_r = R;
+    w.replica_workers.assign(R, 0);
+    w.chain_index_global.assign(R, 0);
+    for (size_t i = 0; i < R; i++) w.chain_index_global[i] = (uint8_t)(i / w.params.Nt);
+    w.chain_index_local = w.chain_index_global;
+    w.beta_values_local = w.beta_values;
 }
-
-void initialize_replicas(PTWorker& w) { check(pticm_init_states(w.ctx, w.params.seed)); }
 
 void sweep_all(PTWorker& w) { check(pticm_run(w.ctx, 1, PTICM_PHASE_SWEEP)); }
 void replica_exchange(PTWorker& w) { check(pticm_run(w.ctx, 1, PTICM_PHASE_EXCHANGE)); }
 void icm_all(PTWorker& w) { check(pticm_run(w.ctx, 1, PTICM_PHASE_ICM)); }
 
 void gather_best_energy_values(PTWorker& w, double& best_ene, size_t& best_sweep, StateVector& best_state) {
+    if (!w.replicas.empty()) {
+        // src/mpi_utils.cc:103-163 over the worker's Replica objects: the
+        // first replica with the lowest best energy
+        best_ene = 1.7976931348623157e308;
+        best_sweep = 0;
+        for (Replica& r : w.replicas) {
+            const double e = r.get_best_ene();
+            if (e < best_ene) {
+                best_ene = e;
+                best_state = r.get_best_state();
+                best_sweep = r.get_best_sweep();
+            }
+        }
+        return;
+    }
     std::vector<uint8_t> s(w.p.vcount());
     uint64_t sweep = 0;
     int64_t rep = -1;
@@ -189,6 +228,13 @@ void gather_best_energy_values(PTWorker& w, double& best_ene, size_t& best_sweep
 }
 
 uint64_t get_flips(PTWorker& w) {
+    if (!w.replicas.empty()) {
+        // src/mpi_utils.cc:167-176 (summed in 64 bits: the reference's int
+        // accumulator wraps past 2^31)
+        uint64_t sum = 0;
+        for (const Replica& r : w.replicas) sum += r.get_flips();
+        return sum;
+    }
     pticm_stats st;
     check(pticm_get_stats(w.ctx, &st, nullptr, nullptr));
     return st.flips;
@@ -209,7 +255,8 @@ static void refresh_exchange(PTWorker& w) {
 
 void solve(PTWorker& w, std::string& problem_path, double& best_ene, size_t& flips, StateVector& best_state) {
     const auto t0 = std::chrono::steady_clock::now();
-    w.p = Problem(problem_path, w.params.seed, w.params.burn_in);
+    read_problem(w, problem_path);
+    w.replicas.clear();
     initialize_temperatures(w);
     bool have_hist = false;
     if (!w.params.resume.empty()) {
@@ -225,7 +272,8 @@ void solve(PTWorker& w, std::string& problem_path, double& best_ene, size_t& fli
         uint64_t nb = 0;
         have_hist = pticm_get_energy_histograms(w.ctx, nullptr, &lo, &nb) == PTICM_OK;
     } else {
-        initialize_replicas(w);
+        // the GPU-resident run draws its initial states on the device
+        check(pticm_init_states(w.ctx, w.params.seed));
     }
     // --log: per-temperature observables from the steps after the burn-in
     if (w.params.log_data && !have_hist) check(pticm_enable_energy_histograms(w.ctx, w.params.burn_in));

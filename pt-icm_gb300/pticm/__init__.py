@@ -53,6 +53,12 @@ class Stats(C.Structure):
                 ("replicas", C.c_uint32), ("last_run_ms", C.c_double)]
 
 
+class Layout(C.Structure):
+    _fields_ = [("replicas_per_block", C.c_uint32), ("blocks", C.c_uint32), ("threads", C.c_uint32),
+                ("icm_teams", C.c_uint32), ("block_team", C.c_int32), ("narrow", C.c_int32),
+                ("adjacency_staged", C.c_int32), ("state_mode", C.c_int32)]
+
+
 class Trace(C.Structure):
     _fields_ = [("pt_steps", C.c_uint64), ("uniforms", C.c_void_p), ("n_uniforms", C.c_uint64),
                 ("sweep_offsets", C.c_void_p), ("xchg_slot", C.c_void_p), ("xchg_logu", C.c_void_p),
@@ -94,6 +100,10 @@ def lib():
         "pticm_checkpoint_save": [P, C.c_char_p],
         "pticm_checkpoint_load": [P, C.c_char_p],
         "pticm_replay": [P, C.POINTER(Trace)],
+        "pticm_icm_pairs": [P, P, u32, C.c_int],
+        "pticm_get_exchange_order": [P, P],
+        "pticm_get_layout": [P, C.POINTER(Layout)],
+        "pticm_set_wait_limit": [P, u64, u32],
         "pticm_philox_probe": [P, P, P, C.c_int],
         "pticm_set_profiling": [P, C.c_int],
         "pticm_cae_ladder": [P, u64, dbl, dbl, C.c_int, u32, dbl, dbl, dbl, u64, u64, P, P],
@@ -103,7 +113,7 @@ def lib():
         "pticm_cae_walk": [P, u64, dbl, dbl, dbl, dbl, dbl, dbl, u32, P, P],
         "pticm_get_profile": [P, P, P],
         "pticm_get_observables": [P, P, P, P, P, P, P],
-        "pticm_tc_gemm_check": [C.c_int, C.c_int, C.c_int, P, P, P, C.c_int, P],
+        "pticm_tc_gemm_check": [C.c_int, C.c_int, C.c_int, P, P, P, C.c_int, P, P],
         "pticm_batch_create": [P, u32, C.POINTER(Opts), C.POINTER(P)],
         "pticm_batch_set_ladders": [P, P, u32, i32],
         "pticm_batch_init_states": [P, u64],
@@ -343,6 +353,31 @@ class Context:
         nc = C.c_uint32()
         _check(lib().pticm_get_ladder(self._h, _p(b), _p(s2r), C.byref(nc)))
         return b, s2r, nc.value
+
+    def icm_pairs(self, seeds, exact=False):
+        """One ICM phase with caller seeds: seeds[q] per pair q (original site,
+        -1 for the engine's draw, -2 to skip); exact flips the seed's cluster
+        itself instead of the smaller side."""
+        sd = np.ascontiguousarray(seeds, np.int64)
+        _check(lib().pticm_icm_pairs(self._h, _p(sd), len(sd), int(exact)))
+
+    def layout(self) -> Layout:
+        """Replicas per block, blocks, threads, ICM teams, block team, narrow
+        kernel, staged adjacency, state mode (0 smem, 1 field gather, 2 global)."""
+        out = Layout()
+        _check(lib().pticm_get_layout(self._h, C.byref(out)))
+        return out
+
+    def exchange_order(self):
+        """The pair order of the reference-order exchange (nt-1 entries)."""
+        o = np.zeros(max(self.nt - 1, 1), np.uint32)
+        _check(lib().pticm_get_exchange_order(self._h, _p(o)))
+        return o[:self.nt - 1]
+
+    def set_wait_limit(self, limit_ns=0, phantom_arrivals=0):
+        """Limit of every wait on other blocks (0: 2 s); phantom_arrivals=1
+        makes every group barrier wait for a block that never comes."""
+        _check(lib().pticm_set_wait_limit(self._h, int(limit_ns), int(phantom_arrivals)))
 
     def set_profiling(self, enable=True):
         _check(lib().pticm_set_profiling(self._h, int(enable)))

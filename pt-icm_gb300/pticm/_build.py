@@ -19,13 +19,14 @@ HOSTSRC = os.path.join(ROOT, "host")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "libpticm_gb300.so")
 CLI = os.path.join(ROOT, "bin", "pt_icm")
+SHIM = os.path.join(PKG, "libpticm_shim.a")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden",
            "--expt-relaxed-constexpr"] + ARCH
 INCS = ["-I", os.path.join(REPO, "include"), "-I", CSRC]
 
-LIB_SOURCES = ["pt_engine.cu", "runtime.cu", "problem_host.cc", "noalloc.cu", "mhist.cu", "mhist_host.cc", "tc_gemm.cu", "mlp.cu", "batch.cu", "surrogate.cu"]
+LIB_SOURCES = ["pt_engine.cu", "runtime.cu", "problem_host.cc", "noalloc.cu", "replica.cu", "mhist.cu", "mhist_host.cc", "tc_gemm.cu", "mlp.cu", "batch.cu", "surrogate.cu"]
 
 
 def nvcc() -> str:
@@ -65,16 +66,44 @@ def build(verbose: bool = False) -> str:
         tmp = LIB + ".tmp"
         subprocess.check_call([nvcc(), "-shared"] + ARCH + ["-o", tmp] + objs + ["-lcudart"])
         os.replace(tmp, LIB)
+    build_shim()
     cli_src = os.path.join(HOSTSRC, "pt_icm_main.cc")
     if os.path.exists(cli_src):
         os.makedirs(os.path.dirname(CLI), exist_ok=True)
-        host_srcs = [os.path.join(HOSTSRC, f) for f in sorted(os.listdir(HOSTSRC)) if f.endswith(".cc")]
-        newest = max(os.path.getmtime(x) for x in host_srcs + [LIB])
+        newest = max(os.path.getmtime(x) for x in [cli_src, SHIM, LIB])
         if not os.path.exists(CLI) or os.path.getmtime(CLI) < newest:
             subprocess.check_call(["g++", "-std=c++17", "-O2", "-I", os.path.join(REPO, "include"),
-                                   "-I", HOSTSRC, "-o", CLI] + host_srcs +
-                                  ["-L", PKG, "-lpticm_gb300", "-Wl,-rpath,$ORIGIN/../pticm"])
+                                   "-I", HOSTSRC, "-o", CLI, cli_src, SHIM,
+                                   "-L", PKG, "-lpticm_gb300", "-Wl,-rpath,$ORIGIN/../pticm"])
     return LIB
+
+
+def build_shim() -> str:
+    """The reference's C++ interface (host/*.cc but the CLI's main) as a
+    static archive, libpticm_shim.a next to the native library: link it and
+    libpticm_gb300.so to build code written against pticm_gb300.hh."""
+    srcs = [os.path.join(HOSTSRC, f) for f in sorted(os.listdir(HOSTSRC))
+            if f.endswith(".cc") and f != "pt_icm_main.cc"]
+    hdrs = [os.path.join(HOSTSRC, f) for f in os.listdir(HOSTSRC) if f.endswith(".hh")]
+    hdrs.append(os.path.join(REPO, "include", "pticm.h"))
+    newest = max(os.path.getmtime(x) for x in srcs + hdrs)
+    if os.path.exists(SHIM) and os.path.getmtime(SHIM) >= newest:
+        return SHIM
+
+    def one(src):
+        obj = os.path.join(BUILD, "shim_" + os.path.basename(src) + ".o")
+        subprocess.check_call(["g++", "-std=c++17", "-O2", "-fPIC", "-I", os.path.join(REPO, "include"),
+                               "-I", HOSTSRC, "-c", src, "-o", obj])
+        return obj
+
+    with cf.ThreadPoolExecutor(max_workers=len(srcs)) as ex:
+        objs = list(ex.map(one, srcs))
+    tmp = SHIM + ".tmp"
+    if os.path.exists(tmp):
+        os.remove(tmp)
+    subprocess.check_call(["ar", "rcs", tmp] + objs)
+    os.replace(tmp, SHIM)
+    return SHIM
 
 
 if __name__ == "__main__":

@@ -70,7 +70,9 @@ RUNS = [
 
 
 def main():
-    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_dir = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PTICM_REFERENCE_DIR")
+    if not ref_dir:
+        sys.exit("usage: make_golden.py REFERENCE_DIR (or set PTICM_REFERENCE_DIR)")
     subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), ref_dir])
     os.makedirs(GRAPHS, exist_ok=True)
     for fname, fac in INSTANCES:

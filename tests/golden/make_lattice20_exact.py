@@ -31,4 +31,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PTICM_REFERENCE_DIR")
+    if not ref:
+        sys.exit("usage: make_lattice20_exact.py REFERENCE_DIR (or set PTICM_REFERENCE_DIR)")
+    main(ref)

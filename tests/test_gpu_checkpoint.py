@@ -92,3 +92,56 @@ def test_checkpoint_refuses_other_contexts(pticm, tmp_path):
     junk.write_bytes(b"not a checkpoint at all")
     with pytest.raises(pticm.PticmError):
         ctx.checkpoint_load(str(junk))
+
+
+def _array_offsets(path, nt):
+    """Byte offsets of the arrays of a checkpoint file, in file order: the
+    header (magic, version, 11 identity words, padding, steps, attempts, nc,
+    the ladder, the histogram range), then u64 byte count + bytes each."""
+    import struct
+    data = open(path, "rb").read()
+    off = 8 + 4 + 4 + 11 * 8 + 8 + 8 + 8 + 8 + nt * 8 + 8 + 8 + 8
+    out = []
+    while off < len(data):
+        (nbytes,) = struct.unpack_from("<Q", data, off)
+        out.append((off + 8, nbytes))
+        off += 8 + nbytes
+    return data, out
+
+
+@pytest.mark.parametrize("which,index", [("slot map", 9), ("exchange order", 10)])
+def test_checkpoint_with_a_broken_permutation_is_refused(pticm, tmp_path, which, index):
+    """The engine indexes with the slot map and the exchange order: a file
+    whose map is not a permutation is refused before anything is uploaded
+    (spins, fields, energies, best states, flips, best sweeps, swap attempts,
+    swap successes, then the slot map and the exchange order)."""
+    import struct
+    prob = pticm.Problem.load(os.path.join(GRAPHS, "rnd200_w1"))
+    ctx = pticm.Context(prob, nt=8, seed=3, icm=True, exchange=0)
+    ctx.set_ladder(pticm.beta_linspace(0.5, 3.0, 8))
+    ctx.init_states(1)
+    ctx.run(10)
+    path = str(tmp_path / "a.ckpt")
+    ctx.checkpoint_save(path)
+    data, arrays = _array_offsets(path, 8)
+    off, nbytes = arrays[index]
+    assert nbytes >= 8
+    bad = bytearray(data)
+    first = struct.unpack_from("<I", bad, off)[0]
+    struct.pack_into("<I", bad, off + 4, first)       # entry 1 repeats entry 0
+    broken = tmp_path / "broken.ckpt"
+    broken.write_bytes(bytes(bad))
+    other = pticm.Context(prob, nt=8, seed=3, icm=True, exchange=0)
+    other.set_ladder(pticm.beta_linspace(0.5, 3.0, 8))
+    with pytest.raises(pticm.PticmError) as e:
+        other.checkpoint_load(str(broken))
+    assert e.value.code == 1 and which in str(e.value) and "permutation" in str(e.value)
+    out_of_range = bytearray(data)
+    struct.pack_into("<I", out_of_range, off, 1000)
+    broken.write_bytes(bytes(out_of_range))
+    with pytest.raises(pticm.PticmError):
+        other.checkpoint_load(str(broken))
+    # the intact file still loads
+    other.checkpoint_load(path)
+    other.run(5)
+    assert other.verify() == 0

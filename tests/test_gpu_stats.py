@@ -7,7 +7,17 @@ each neighbouring pair must agree within 3 sigma of their seed-to-seed
 spread (at most one of all comparisons beyond 3 sigma, none beyond 4.5).
 Both production exchange orders are checked.  On small instances the best
 energy found must equal the oracle's best.
+
+The larger shapes -- the +-J L=20 lattice on the C1 ladder (32 temperatures),
+a 1000-site +-1 graph and the C2 shape (N=2000, M=19990, 64 temperatures),
+all with ICM on -- compare against oracle statistics committed in
+tests/golden/stats_*.json (made by tests/golden/make_stats.py: 16 seeds of
+long oracle runs).  They run the block-team kernel (one replica per block,
+the layout of the C1/C2 workloads) and, where the replicas fit, several
+replicas per block with warp or block-wide ICM teams.
 """
+import json
+import math
 import os
 
 import numpy as np
@@ -88,3 +98,68 @@ def test_best_energy_matches_reference_on_small_instances(g, nt, T0, T1):
     assert out["best_energy"] == best_ref
     E, cut = prob.evaluate(out["best_state"][None, :])
     assert E[0] == out["best_energy"]
+
+
+STATS = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _fixture(name):
+    with open(os.path.join(STATS, f"stats_{name}.json")) as f:
+        return json.load(f)
+
+
+def _fixture_graph(name, fx, tmp_path):
+    import hashlib
+    if name == "c2":
+        from pticm import instances
+        path = instances.c2().write_gset(str(tmp_path / "c2"))
+    else:
+        path = os.path.join(G, fx["config"]["graph"])
+    with open(path, "rb") as f:
+        assert hashlib.sha256(f.read()).hexdigest() == fx["graph_sha256"], "not the graph the oracle ran"
+    return path
+
+
+def _gpu_block_runs(path, c, seeds, exchange, rpb):
+    import pticm
+    prob = pticm.Problem.load(path)
+    nt = c["nt"]
+    beta = pticm.beta_linspace(c["T0"], c["T1"], nt)
+    means, rates, nc, lay = [], [], None, None
+    for s in range(seeds):
+        ctx = pticm.Context(prob, nt=nt, seed=900 + s, icm=True, exchange=exchange, replicas_per_block=rpb)
+        ctx.set_ladder(beta)
+        ctx.init_states(900 + s)
+        ctx.enable_energy_histograms(c["burn"])
+        ctx.run(c["pts"])
+        assert ctx.verify() == 0
+        lay = ctx.layout()
+        h, e = ctx.energy_histograms()
+        m = (h * e[None, :]).sum(axis=1) / h.sum(axis=1)
+        means.append(m.reshape(2, nt).mean(axis=0))
+        st, att, suc = ctx.stats()
+        nc = st.nc
+        att = att.astype(float)
+        suc = suc.astype(float)
+        rates.append((suc[:nt - 1] + suc[nt:2 * nt - 1]) / np.maximum(att[:nt - 1] + att[nt:2 * nt - 1], 1))
+    return np.array(means), np.array(rates), nc, lay
+
+
+@pytest.mark.parametrize("exchange", [1, 0])
+@pytest.mark.parametrize("name,rpb", [("pmL20_c1", 1), ("pmL20_c1", 8), ("rnd200_w1", 1), ("rnd200_w1", 4),
+                                      ("rnd1000_pm", 1), ("rnd1000_pm", 4), ("c2", 1)])
+def test_block_layouts_match_oracle_statistics(name, rpb, exchange, tmp_path):
+    fx = _fixture(name)
+    c = fx["config"]
+    path = _fixture_graph(name, fx, tmp_path)
+    gm, grate, nc, lay = _gpu_block_runs(path, c, 16, exchange, rpb)
+    assert nc == fx["nc"] > 0, "ICM pairs differ from the reference's count"
+    assert lay.replicas_per_block == rpb
+    if rpb == 1:
+        assert lay.block_team == 1, "one replica per block runs the block-team kernel"
+    om = np.array(fx["mean_energy"])
+    orate = np.array(fx["acceptance"])
+    z = np.concatenate([_agree(gm, om), _agree(grate, orate)])
+    allowed = max(1, math.ceil(0.02 * len(z)))
+    assert (z > 3.0).sum() <= allowed, (np.round(z, 2), allowed)
+    assert z.max() < 4.5, np.round(z, 2)

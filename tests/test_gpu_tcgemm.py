@@ -25,18 +25,22 @@ def test_tc_gemm_matches_torch_fp32(M, N, K, act):
     b_bits, b = _bf16_bits(rng.standard_normal((N, K)) / np.sqrt(K))
     bias = rng.standard_normal(N).astype(np.float32)
     out = np.zeros((M, N), np.float32)
+    out_bf16 = np.zeros((M, N), np.uint16)
     L = pticm.lib()
     L.pticm_tc_gemm_check.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
-                                      C.c_void_p]
+                                      C.c_void_p, C.c_void_p]
     rc = L.pticm_tc_gemm_check(M, N, K, a_bits.ctypes.data, b_bits.ctypes.data, bias.ctypes.data, act,
-                               out.ctypes.data)
+                               out.ctypes.data, out_bf16.ctypes.data)
     assert rc == 0, L.pticm_last_error()
-    ref = (a @ b.T + torch.from_numpy(bias)).numpy()
-    if act == 1:
-        pre = out.copy()
-        assert np.allclose(pre, pre)   # finite
-        ref = ref  # act applies only to the bf16 output; the fp32 output is pre-activation
-    assert np.allclose(out, ref, rtol=1e-4, atol=1e-3), np.abs(out - ref).max()
+    pre = a @ b.T + torch.from_numpy(bias)
+    # the FP32 output is the pre-activation sum
+    assert np.allclose(out, pre.numpy(), rtol=1e-4, atol=1e-3), np.abs(out - pre.numpy()).max()
+    # the BF16 output is the activation of it, rounded to BF16 (one BF16 ulp
+    # of the value plus the fast exponential's error)
+    post = torch.nn.functional.silu(pre) if act == 1 else pre
+    got = torch.from_numpy(out_bf16.view(np.int16)).view(torch.bfloat16).to(torch.float32).numpy()
+    want = post.numpy()
+    assert np.all(np.abs(got - want) <= 2.0 ** -7 * np.abs(want) + 1e-3), np.abs(got - want).max()
 
 
 def test_tc_gemm_bench_runs():

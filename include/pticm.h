@@ -228,12 +228,17 @@ PTICM_API int pticm_verify(pticm_ctx* c, uint64_t* mismatches);
 /* Phase timers (tracing): when enabled, every block of the following
  * pticm_run calls accumulates clock64 cycles spent in the sweep, the
  * publish+barrier, the exchange and the ICM phases, and the whole launch,
- * then ICM split into overlap, seed choice, union, flip and energies, and
- * the exchange split into draws, dependency levels, attempts and reshuffle
- * (PTICM_PROFILE_SLOTS values).  pticm_get_profile converts them to
- * milliseconds at the device's maximum SM clock and reports the mean and
- * the maximum over blocks; enabling again clears the counters. */
-#define PTICM_PROFILE_SLOTS 14
+ * then ICM split into overlap, seed choice, union, flip and energies, the
+ * exchange split into draws, dependency levels, attempts and reshuffle, the
+ * union-find labelling of a block-wide ICM team split into its first link
+ * round, compression, second link round, giant-component vote, the pass
+ * listing the sites outside the giant component, their unions and the
+ * cluster size, and the sweep time of blocks whose replica is in an ICM pair
+ * of the step (PTICM_PROFILE_SLOTS values).  pticm_get_profile converts them
+ * to milliseconds at the device's maximum SM clock and reports the mean and
+ * the maximum over blocks -- except the last slot, the number of ICM pairs
+ * with a nonempty overlap a block ran; enabling again clears the counters. */
+#define PTICM_PROFILE_SLOTS 23
 PTICM_API int pticm_set_profiling(pticm_ctx* c, int enable);
 PTICM_API int pticm_get_profile(pticm_ctx* c, double* mean_ms, double* max_ms);
 

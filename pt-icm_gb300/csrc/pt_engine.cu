@@ -474,6 +474,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                         if (tgt >= 0) ok &= uf_unite(lab, u, tgt);
                     });
                     team.sync();
+                    if (threadIdx.x == 0) P.subtick(round == 0 ? PROF_UF_LINK0 : PROF_UF_LINK1);
                     if (round == 0) {
                         // (after the last round the vote's and phase 3's
                         // finds halve the paths they walk)
@@ -483,6 +484,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                             else vl[u] = r;
                         });
                         team.sync();
+                        if (threadIdx.x == 0) P.subtick(PROF_UF_COMPRESS);
                     }
                 }
                 if (team.tr < 32) {
@@ -516,6 +518,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                     if (team.tr == 0) team.ctl[0] = best;
                 }
                 team.sync();
+                if (threadIdx.x == 0) P.subtick(PROF_UF_VOTE);
                 const int L = *(volatile int*)team.ctl;
                 for_overlap([&](int u) {
                     if (uf_find(vl, u) == L) return;
@@ -533,6 +536,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                     }
                 });
                 team.sync();
+                if (threadIdx.x == 0) P.subtick(PROF_UF_OUTSIDE);
                 if (BLOCK) {
                     // the edges of S: one warp per site and one lane per
                     // neighbour (the unions of a site side by side) when
@@ -551,6 +555,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                         }
                     }
                     team.sync();
+                    if (threadIdx.x == 0) P.subtick(PROF_UF_SUNION);
                 }
                 if (BLOCK) {
                     // sites in L's component at their phase-3 check stay in it:
@@ -570,6 +575,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                     fast = (rs == rL) ? sw : !sw;   // the flipped set lies in S
                     fast_root = rs == rL ? rL : rs;
                     fast_eq = rs != rL;
+                    if (threadIdx.x == 0) P.subtick(PROF_UF_SIZE);
                 }
             } else {
                 // minimum-label propagation with root hooking and pointer jumping
@@ -745,7 +751,10 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
         team.ctl[4] = 0;
     }
     team.sync();
-    if (threadIdx.x == 0) P.subtick(PROF_ICM_FLIP);
+    if (threadIdx.x == 0) {
+        P.subtick(PROF_ICM_FLIP);
+        if (P.on && cnt > 0) P.c[PROF_ICM_COUNT]++;
+    }
     return swapped;
 }
 
@@ -1318,6 +1327,9 @@ __global__ void __launch_bounds__((REPLAY || (BLOCKTEAM && !NARROW)) ? 1024 : kN
         }
         const unsigned long long step = A.step0 + (unsigned long long)ls;
         const int parity = (int)(step & 1ull);
+        // (profiling) a block holding one replica at an ICM temperature
+        const bool cold = P.on && icm_on && rpc == 1 && (nt - 1 - (int)(B.rslot[0] % (uint32_t)nt)) < D.nc;
+        const long long t_sw = P.on ? clock64() : 0;
         if (A.phase_mask & PHASE_SWEEP) {
             for (int sw = 0; sw < A.sweeps; sw++) {
                 const unsigned long long sweep_idx = step * (unsigned long long)A.sweeps + (unsigned long long)sw;
@@ -1331,6 +1343,7 @@ __global__ void __launch_bounds__((REPLAY || (BLOCKTEAM && !NARROW)) ? 1024 : kN
             }
         }
         P.tick(PROF_SWEEP);
+        if (cold) P.c[PROF_SWEEP_ICM] += clock64() - t_sw;
         const bool observe = A.obs != nullptr && D.hist_nbins > 0 && step >= A.hist_from;
         if (observe) {
             // magnetisation of the block's replicas, one warp per replica

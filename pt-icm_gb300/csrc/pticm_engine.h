@@ -199,12 +199,19 @@ enum PhaseBits : int32_t { PHASE_SWEEP = 1, PHASE_EXCHANGE = 2, PHASE_ICM = 4 };
 // and ICM, plus the whole launch.
 // Slots 5.. split ICM (overlap+count, seed choice, union, flip, energies) and
 // the exchange (draws, dependency levels, attempts, reshuffle) as seen by
-// thread 0 of the block.
+// thread 0 of the block; slots 14-20 split the union-find labelling of a
+// block team (the two link rounds and the compression between them, the
+// vote for the giant component, the pass that lists the sites outside it,
+// their unions, and the cluster size), slot 21 is the sweep time of blocks
+// whose replica takes part in an ICM pair of the step, and slot 22 counts
+// the ICM pairs with a nonempty overlap (a count, not cycles).
 enum ProfSlots : int32_t {
     PROF_SWEEP = 0, PROF_BARRIER = 1, PROF_EXCHANGE = 2, PROF_ICM = 3, PROF_TOTAL = 4,
     PROF_ICM_DIFF = 5, PROF_ICM_SEED = 6, PROF_ICM_UNION = 7, PROF_ICM_FLIP = 8, PROF_ICM_ENERGY = 9,
     PROF_X_DRAW = 10, PROF_X_LEVELS = 11, PROF_X_APPLY = 12, PROF_X_SHUFFLE = 13,
-    PROF_PHASES = 14
+    PROF_UF_LINK0 = 14, PROF_UF_COMPRESS = 15, PROF_UF_LINK1 = 16, PROF_UF_VOTE = 17, PROF_UF_OUTSIDE = 18,
+    PROF_UF_SUNION = 19, PROF_UF_SIZE = 20, PROF_SWEEP_ICM = 21, PROF_ICM_COUNT = 22,
+    PROF_PHASES = 23
 };
 
 }  // namespace pticm

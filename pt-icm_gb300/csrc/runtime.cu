@@ -1259,7 +1259,7 @@ int pticm_set_profiling(pticm_ctx* c, int enable) {
 }
 
 int pticm_get_profile(pticm_ctx* c, double* mean_ms, double* max_ms) {
-    static_assert(PROF_PHASES == 14, "profile slots");
+    static_assert(PROF_PHASES == PTICM_PROFILE_SLOTS, "profile slots");
     if (!c) return fail(PTICM_ERR_INVALID, "null argument");
     if (!c->profiling) return fail(PTICM_ERR_INVALID, "profiling is not enabled");
     CK(cudaStreamSynchronize(c->stream));
@@ -1273,7 +1273,8 @@ int pticm_get_profile(pticm_ctx* c, double* mean_ms, double* max_ms) {
     for (int q = 0; q < PROF_PHASES; q++) {
         double sum = 0, mx = 0;
         for (int b = 0; b < blocks; b++) {
-            const double x = (double)v[(size_t)b * PROF_PHASES + q] * to_ms;
+            const double raw = (double)v[(size_t)b * PROF_PHASES + q];
+            const double x = q == PROF_ICM_COUNT ? raw : raw * to_ms;
             sum += x;
             mx = std::max(mx, x);
         }

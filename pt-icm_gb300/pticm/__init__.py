@@ -383,12 +383,15 @@ class Context:
         _check(lib().pticm_set_profiling(self._h, int(enable)))
 
     def profile(self):
-        """Mean and max over blocks of ms in (sweep, barrier, exchange, ICM, total)."""
-        mean = np.zeros(14)
-        mx = np.zeros(14)
+        """Mean and max over blocks of ms per phase (the last entry, icm_pairs,
+        counts ICM pairs with a nonempty overlap)."""
+        mean = np.zeros(23)
+        mx = np.zeros(23)
         _check(lib().pticm_get_profile(self._h, _p(mean), _p(mx)))
         names = ("sweep", "barrier", "exchange", "icm", "total", "icm_diff", "icm_seed", "icm_union",
-                 "icm_flip", "icm_energy", "x_draw", "x_levels", "x_apply", "x_shuffle")
+                 "icm_flip", "icm_energy", "x_draw", "x_levels", "x_apply", "x_shuffle", "uf_link0",
+                 "uf_compress", "uf_link1", "uf_vote", "uf_outside", "uf_s_unions", "uf_size", "sweep_icm",
+                 "icm_pairs")
         return dict(zip(names, mean)), dict(zip(names, mx))
 
     def enable_energy_histograms(self, from_step=0):

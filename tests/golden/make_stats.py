@@ -5,10 +5,14 @@ pinned to the reference build) for several seeds of each configuration and
 stores, per seed, the per-temperature mean energy after the burn-in (slot
 energies after the sweeps of each step, both chains merged) and the exchange
 acceptance of every neighbouring pair (both chains merged), as the GPU test
-computes them.  The windows are long enough for the two halves of each to
-agree (half_window_z_max): the engine's colour-class sweeps and the
-reference's sequential sweeps share the stationary distribution but relax
-at different rates, so only equilibrium statistics are comparable.  The
+computes them.  Only equilibrium statistics are comparable: the engine's
+colour-class sweeps and the reference's sequential sweeps share the
+stationary distribution but relax at different rates.  So the fixture also
+stores, per temperature, how far the mean energies of the two halves of the
+window are apart (half_window_z, in units of their seed-to-seed spread); the
+coldest temperatures of the glassy C2 instance are still relaxing after
+64000 steps, and the tests compare only the temperatures where the two
+halves agree.  The
 runs are long at the C2 shape (16 ms a PT step on one core), so they are
 made once here and committed as stats_<name>.json.
 
@@ -41,7 +45,7 @@ CONFIGS = {
     "pmL20_c1": dict(graph="pmL20_c1.gset", nt=32, T0=0.5, T1=3.0, pts=30000, burn=15000),
     "rnd200_w1": dict(graph="rnd200_w1", nt=10, T0=0.5, T1=15.0, pts=8000, burn=4000),
     "rnd1000_pm": dict(graph="rnd1000_pm", nt=24, T0=0.5, T1=5.0, pts=16000, burn=8000),
-    "c2": dict(graph="c2", nt=64, T0=0.5, T1=15.0, pts=16000, burn=8000),
+    "c2": dict(graph="c2", nt=64, T0=0.5, T1=15.0, pts=64000, burn=32000),
 }
 
 
@@ -99,7 +103,7 @@ def main():
             out = dict(config=c, graph_sha256=file_digest(path), seeds=[r[0] for r in res],
                        mean_energy=[r[1] for r in res], acceptance=[r[2] for r in res],
                        best_energy=[r[3] for r in res], nc=res[0][4],
-                       half_window_z_max=float(zh.max()),
+                       half_window_z=zh.tolist(), half_window_z_max=float(zh.max()),
                        made_by="tests/golden/make_stats.py (C oracle, energies after the sweeps of each step)")
             with open(os.path.join(HERE, f"stats_{name}.json"), "w") as f:
                 json.dump(out, f)

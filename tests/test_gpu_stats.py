@@ -14,7 +14,13 @@ all with ICM on -- compare against oracle statistics committed in
 tests/golden/stats_*.json (made by tests/golden/make_stats.py: 16 seeds of
 long oracle runs).  They run the block-team kernel (one replica per block,
 the layout of the C1/C2 workloads) and, where the replicas fit, several
-replicas per block with warp or block-wide ICM teams.
+replicas per block with warp or block-wide ICM teams.  Mean energies are
+compared at the temperatures where the reference algorithm is at
+equilibrium over the window (its two halves agree): the engine's
+colour-class sweeps and the reference's sequential sweeps share the
+stationary distribution but not the relaxation, and the coldest
+temperatures of the glassy C2 instance still relax after 16000 steps.  The
+lowest energy of the 16 GPU runs must reach the reference runs' best.
 """
 import json
 import math
@@ -125,7 +131,7 @@ def _gpu_block_runs(path, c, seeds, exchange, rpb):
     prob = pticm.Problem.load(path)
     nt = c["nt"]
     beta = pticm.beta_linspace(c["T0"], c["T1"], nt)
-    means, rates, nc, lay = [], [], None, None
+    means, rates, nc, lay, best = [], [], None, None, []
     for s in range(seeds):
         ctx = pticm.Context(prob, nt=nt, seed=900 + s, icm=True, exchange=exchange, replicas_per_block=rpb)
         ctx.set_ladder(beta)
@@ -142,7 +148,8 @@ def _gpu_block_runs(path, c, seeds, exchange, rpb):
         att = att.astype(float)
         suc = suc.astype(float)
         rates.append((suc[:nt - 1] + suc[nt:2 * nt - 1]) / np.maximum(att[:nt - 1] + att[nt:2 * nt - 1], 1))
-    return np.array(means), np.array(rates), nc, lay
+        best.append(ctx.best()[0])
+    return np.array(means), np.array(rates), nc, lay, np.array(best)
 
 
 @pytest.mark.parametrize("exchange", [1, 0])
@@ -152,14 +159,22 @@ def test_block_layouts_match_oracle_statistics(name, rpb, exchange, tmp_path):
     fx = _fixture(name)
     c = fx["config"]
     path = _fixture_graph(name, fx, tmp_path)
-    gm, grate, nc, lay = _gpu_block_runs(path, c, 16, exchange, rpb)
+    gm, grate, nc, lay, gbest = _gpu_block_runs(path, c, 16, exchange, rpb)
     assert nc == fx["nc"] > 0, "ICM pairs differ from the reference's count"
     assert lay.replicas_per_block == rpb
     if rpb == 1:
         assert lay.block_team == 1, "one replica per block runs the block-team kernel"
     om = np.array(fx["mean_energy"])
     orate = np.array(fx["acceptance"])
-    z = np.concatenate([_agree(gm, om), _agree(grate, orate)])
+    # equilibrium temperatures: the reference algorithm's mean energies over
+    # the two halves of the window agree (the coldest temperatures of the
+    # glassy C2 instance are still relaxing); pairs of two such temperatures
+    eq = np.array(fx["half_window_z"]) < 3.0
+    assert eq.sum() >= (0.5 if name == "c2" else 0.85) * len(eq), "too few equilibrated temperatures"
+    eq_pairs = eq[:-1] & eq[1:]
+    z = np.concatenate([_agree(gm[:, eq], om[:, eq]), _agree(grate[:, eq_pairs], orate[:, eq_pairs])])
+    # the best energy of the reference algorithm's runs is reached
+    assert gbest.min() <= min(fx["best_energy"]), (gbest, fx["best_energy"])
     allowed = max(1, math.ceil(0.02 * len(z)))
     assert (z > 3.0).sum() <= allowed, (np.round(z, 2), allowed)
     assert z.max() < 4.5, np.round(z, 2)

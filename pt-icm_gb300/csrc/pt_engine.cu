@@ -218,7 +218,7 @@ __device__ __forceinline__ void for_each_neighbour(const int32_t* row, const uin
 // the set (s_v equal in A and B), an exact integer update.  Members held by
 // another block are read from the published copy and flipped by their own
 // block, which finds the same set.
-template <bool BLOCK, bool REPLAY>
+template <bool BLOCK, bool REPLAY, bool LS>
 __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK>& team, int q,
                          int rA, int rB, unsigned long long step, int ls, const IcmScratch& X,
                          int where_err, Prof& P) {
@@ -293,24 +293,92 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
         if (valid && di && pf < n) lst[pf] = i;
         if (valid && !di && pb >= 0) lst[pb] = i;
     };
-    // two sites per round, both loaded first: the partner's spins come from
-    // the published copy in L2
-    for (int base = 0; base < n; base += 2 * team.ts) {
-        const int i = base + team.tr, i2 = i + team.ts;
-        int8_t a = 0, b = 0, a2 = 0, b2 = 0;
-        if (i < n) {
-            a = locA ? sA[i] : ld_cg(pubA + i);
-            b = locB ? sB[i] : ld_cg(pubB + i);
+    if (BLOCK && LS) {
+        // four sites per thread: one 32-bit word of each replica's spins (the
+        // partner's from the published copy in L2, one load for all four),
+        // the overlap flags stored as one word, and the sites appended to
+        // the list with one warp scan and one atomic per warp and list
+        // (rows are n_pad bytes, a multiple of 16: every word is aligned)
+        const int lane = threadIdx.x & 31;
+        const int nq = (n + 3) >> 2;
+        for (int w0 = 0; w0 < nq; w0 += team.ts) {
+            const int w = w0 + team.tr;
+            const bool have = w < nq;
+            uint32_t wa = 0, wb = 0;
+            if (have) {
+                wa = locA ? reinterpret_cast<const uint32_t*>(sA)[w]
+                          : __ldcg(reinterpret_cast<const unsigned int*>(pubA) + w);
+                wb = locB ? reinterpret_cast<const uint32_t*>(sB)[w]
+                          : __ldcg(reinterpret_cast<const unsigned int*>(pubB) + w);
+            }
+            uint32_t dw = 0;
+            int fm = 0, bm = 0;
+            if (have) {
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int i = 4 * w + j;
+                    if (i >= n) break;
+                    const int8_t a = (int8_t)(wa >> (8 * j)), b = (int8_t)(wb >> (8 * j));
+                    const bool di = a != b;
+                    dw |= (uint32_t)di << (8 * j);
+                    fm |= (int)di << j;
+                    bm |= (int)!di << j;
+                    cnt += di;
+                    const unsigned long long key =
+                        (mix64(r64 + 0x9E3779B97F4A7C15ull * (unsigned long long)(i + 1)) & 0xFFFFFFFF00000000ull) |
+                        (unsigned)i;
+                    if (di) kd = min(kd, key);
+                    else ke = min(ke, key);
+                    if (D.has_h && locA) hs += (long long)B.h[i] * a;
+                }
+                reinterpret_cast<uint32_t*>(d)[w] = dw;
+                if (algo == ENGINE_ICM_UNION_FIND)   // union-find parents
+                    reinterpret_cast<int4*>(X.queue)[w] = make_int4(4 * w, 4 * w + 1, 4 * w + 2, 4 * w + 3);
+            }
+            // list positions: both counts packed in one int, one inclusive scan
+            const int packed = __popc(fm) | (__popc(bm) << 16);
+            int incl = packed;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            int base_f = 0, base_b = 0;
+            if (lane == 31) {
+                if (incl & 0xffff) base_f = atomicAdd(team.ctl + 2, incl & 0xffff);
+                if (incl >> 16) base_b = atomicAdd(team.ctl + 3, incl >> 16);
+            }
+            base_f = __shfl_sync(0xffffffffu, base_f, 31);
+            base_b = __shfl_sync(0xffffffffu, base_b, 31);
+            const int excl = incl - packed;
+            int pf = base_f + (excl & 0xffff), pb = n - 1 - (base_b + (excl >> 16));
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                if ((fm >> j) & 1) lst[pf++] = 4 * w + j;
+                if ((bm >> j) & 1) lst[pb--] = 4 * w + j;
+            }
         }
-        if (i2 < n) {
-            a2 = locA ? sA[i2] : ld_cg(pubA + i2);
-            b2 = locB ? sB[i2] : ld_cg(pubB + i2);
-        }
-        if (i < n) overlap_site(i, a, b);
-        if (i2 < n) overlap_site(i2, a2, b2);
-        if (BLOCK) {
-            append(i < n, a != b, i);
-            append(i2 < n, a2 != b2, i2);
+    } else {
+        // two sites per round, both loaded first: the partner's spins come
+        // from the published copy in L2 (the wide 1024-thread variants keep
+        // this shorter code, which needs fewer registers)
+        for (int base = 0; base < n; base += 2 * team.ts) {
+            const int i = base + team.tr, i2 = i + team.ts;
+            int8_t a = 0, b = 0, a2 = 0, b2 = 0;
+            if (i < n) {
+                a = locA ? sA[i] : ld_cg(pubA + i);
+                b = locB ? sB[i] : ld_cg(pubB + i);
+            }
+            if (i2 < n) {
+                a2 = locA ? sA[i2] : ld_cg(pubA + i2);
+                b2 = locB ? sB[i2] : ld_cg(pubB + i2);
+            }
+            if (i < n) overlap_site(i, a, b);
+            if (i2 < n) overlap_site(i2, a2, b2);
+            if (BLOCK) {
+                append(i < n, a != b, i);
+                append(i2 < n, a2 != b2, i2);
+            }
         }
     }
     if (algo == ENGINE_ICM_BFS)   // the visited bits of the breadth-first search
@@ -767,6 +835,12 @@ __device__ __forceinline__ int gather_field(const int32_t* row, const uint32_t* 
 }
 
 // --------------------------------------------------------------- sweeps
+// A warp pushes the field changes of at most this many accepted sites one
+// site at a time (a lane per neighbour); with more, each lane pushes its own
+// (on C2, 4 to 8 measured best: 26.5 us per PT step against 27.6 with every
+// lane pushing its own).
+constexpr int kCoopPushSites = 4;
+
 // Colour-class Metropolis sweep of the block's replicas (production).
 // dE_i = -2 s_i (h_i + f_i); accepted with probability min(1, exp(-beta dE))
 // (src/replica.cc:31-38); an accepted flip pushes J_ij * (-2 s_i) into each
@@ -774,7 +848,7 @@ __device__ __forceinline__ int gather_field(const int32_t* row, const uint32_t* 
 // replica per block (ONE) every thread keeps its energy change and flip
 // count in registers until a phase boundary; with several, warps aggregate
 // per replica before touching shared memory.
-template <bool ONE>
+template <bool ONE, bool COOP>
 __device__ void colored_sweep(const EngineArgs& A, const BlockCtx& B, unsigned long long sweep_idx,
                               int32_t* s_col, const uint32_t* s_thr, int* s_dEp, unsigned* s_flp,
                               unsigned long long* s_flips, long long* s_bestE, int* s_improved,
@@ -794,7 +868,58 @@ __device__ void colored_sweep(const EngineArgs& A, const BlockCtx& B, unsigned l
     for (int c = 0; c < D.ncolors; c++) {
         const int c0 = s_col[c];
         const int Sc = s_col[c + 1] - c0;
-        if (ONE) {
+        if (ONE && COOP && B.field) {
+            // each thread decides its own site (the same site and random
+            // draws as one site per thread).  A warp with few accepted sites
+            // (the cold replicas) pushes their field changes one site at a
+            // time with a lane per neighbour, so that no lane walks a long
+            // neighbour list alone; a warp with many (the hot replicas)
+            // lets every lane push its own site's changes, side by side
+            int8_t* sp = B.spin;
+            int32_t* fd = B.field;
+            const uint32_t* thr_row = s_thr + B.tb[0];
+            for (int base = c0 + (tid & ~31); base < c0 + Sc; base += T) {
+                const int i = base + lane;
+                bool acc = false;
+                int s = 0, e0 = 0, e1 = 0;
+                if (i < c0 + Sc) {
+                    s = sp[i];
+                    const int f = fd[i] + (D.has_h ? B.h[i] : 0);
+                    const int de = -2 * s * f;
+                    acc = de <= 0;
+                    if (!acc) {
+                        const uint32_t thr = thr_row[min(de >> 1, kmax)];
+                        acc = (rng.next() < thr) || (thr == 0xFFFFFFFFu);
+                    }
+                    if (acc) {
+                        sp[i] = (int8_t)-s;
+                        acc_de += de;
+                        acc_fl++;
+                        e0 = row[i];
+                        e1 = row[i + 1];
+                    }
+                }
+                unsigned m = __ballot_sync(0xffffffffu, acc);
+                if (__popc(m) > kCoopPushSites) {
+                    if (acc) {
+                        const int dl = -2 * s;
+                        for_each_neighbour(row, adj, i,
+                                           [&](uint32_t e) { atomicAdd(fd + (e >> 8), (int)(int8_t)(e & 0xffu) * dl); });
+                    }
+                    m = 0;
+                }
+                while (m) {
+                    const int src = __ffs(m) - 1;
+                    m &= m - 1;
+                    const int a0 = __shfl_sync(0xffffffffu, e0, src), a1 = __shfl_sync(0xffffffffu, e1, src);
+                    const int dl = -2 * __shfl_sync(0xffffffffu, s, src);
+                    for (int a = a0 + lane; a < a1; a += 32) {
+                        const uint32_t e = adj[a];
+                        atomicAdd(fd + (e >> 8), (int)(int8_t)(e & 0xffu) * dl);
+                    }
+                }
+            }
+        } else if (ONE) {
             int8_t* sp = B.spin;
             int32_t* fd = B.field;   // null in field_gather mode
             const uint32_t* thr_row = s_thr + B.tb[0];
@@ -1337,7 +1462,7 @@ __global__ void __launch_bounds__((REPLAY || (BLOCKTEAM && !NARROW)) ? 1024 : kN
                     replay_sweep(A, B, ls, sw, sweep_idx, s_ptab, s_flips, s_bestE);
                     __syncthreads();
                 } else {
-                    colored_sweep<BLOCKTEAM>(A, B, sweep_idx, s_col, s_thr, s_dEp, s_flp, s_flips, s_bestE,
+                    colored_sweep<BLOCKTEAM, BLOCKTEAM && NARROW>(A, B, sweep_idx, s_col, s_thr, s_dEp, s_flp, s_flips, s_bestE,
                                              s_improved, s_misc, best_pp);
                 }
             }
@@ -1424,7 +1549,8 @@ __global__ void __launch_bounds__((REPLAY || (BLOCKTEAM && !NARROW)) ? 1024 : kN
                     const int cp = c >> 1;
                     const int rA = (int)B.slot[(2 * cp) * nt + k], rB = (int)B.slot[(2 * cp + 1) * nt + k];
                     if ((c & 1) && rA >= B.r0 && rA < B.r0 + rpc) continue;
-                    icm_pair<true, REPLAY>(A, B, team, cp * D.nc + kk, rA, rB, step, ls, X, 30, P);
+                    icm_pair<true, REPLAY, !REPLAY && (NARROW || !BLOCKTEAM)>(A, B, team, cp * D.nc + kk, rA, rB,
+                                                                             step, ls, X, 30, P);
                 }
             } else {
                 const int warp = tid >> 5, lane = tid & 31;
@@ -1440,7 +1566,7 @@ __global__ void __launch_bounds__((REPLAY || (BLOCKTEAM && !NARROW)) ? 1024 : kN
                         const int rA = (int)B.slot[(2 * cp) * nt + k], rB = (int)B.slot[(2 * cp + 1) * nt + k];
                         if ((c & 1) && rA >= B.r0 && rA < B.r0 + rpc) continue;
                         if ((e++ % teams) != warp) continue;
-                        icm_pair<false, REPLAY>(A, B, team, cp * D.nc + kk, rA, rB, step, ls, X, 30, P);
+                        icm_pair<false, REPLAY, false>(A, B, team, cp * D.nc + kk, rA, rB, step, ls, X, 30, P);
                     }
                 }
             }

@@ -38,19 +38,32 @@ for _p in (ROOT, os.path.join(ROOT, "pt-icm_gb300")):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
-N_SPINS, M_EDGES, NT, T0, T1 = 2000, 19990, 64, 0.5, 15.0
 PT_PER_STEP = 1000
 METRIC = "spin-flip attempts/s"
 WORKLOAD = ("random MaxCut N=2000 M=19990 w=+1 (seed 2), Nt=64 x 2 chains (R=128), "
             "T 0.5..15 linear in beta, ICM on, 1 sweep per PT step, 1000 PT steps per bench step")
+C1_WORKLOAD = ("+-J toroidal lattice L=20 (N=400, M=800, seed 1), Nt=32 x 2 chains (R=64), "
+               "T 0.5..3.0 linear in beta, ICM on, 1 sweep per PT step, 1000 PT steps per bench step")
+
+# The single-instance workloads: graph, ladder, the reference arm's PT steps
+# per process per bench step, and the ncu summary that holds the traffic.
+SPECS = {
+    "c2": dict(graph="c2", fname="c2", n=2000, m=19990, nt=64, T0=0.5, T1=15.0, workload=WORKLOAD, ref_pts=20,
+               profile="pt_engine_c2_bench.md"),
+    "c1": dict(graph="c1", fname="c1.gset", n=400, m=800, nt=32, T0=0.5, T1=3.0, workload=C1_WORKLOAD, ref_pts=200,
+               profile="pt_engine_c1_bench.md"),
+}
+# PT steps the CPU legs run untimed before the timed window (the oracle's
+# cost per step settles after a few hundred steps from the random start)
+CPU_WARM_PTS = 300
 
 
-def _graph():
+def _graph(spec):
     from pticm import instances
-    return instances.c2()
+    return getattr(instances, spec["graph"])()
 
 
-def _profiled_traffic(summary="pt_engine_c2_bench.md"):
+def _profiled_traffic(summary):
     """DRAM bytes per engine launch from a committed ncu summary."""
     try:
         with open(os.path.join(ROOT, "profiles", summary)) as f:
@@ -148,71 +161,77 @@ def job_throughput(world, units_per_rank, max_ms):
 
 # ---------------------------------------------------------------- CPU legs
 def _cpu_sample(args):
-    """One oracle solve on a bounded sample of the workload (worker)."""
-    seed, pts, path = args
+    """One oracle solve (worker): CPU_WARM_PTS + warm PT steps untimed, then
+    `timed` PT steps timed inside the oracle's main loop."""
+    seed, warm, timed, path, nt, T0, T1 = args
     from oracle import pyoracle as O
     O.build()
     p = O.Problem.load(path, seed)
-    t = time.perf_counter()
-    O.solve(p, seed=seed, Nt=NT, pts=pts, icm=True, T0=T0, T1=T1)
-    return time.perf_counter() - t
+    sec, _ = O.solve_timed(p, seed=seed, Nt=nt, pts=CPU_WARM_PTS + warm + timed, timed_from=CPU_WARM_PTS + warm,
+                           icm=True, T0=T0, T1=T1)
+    return sec
 
 
-def _write_graph_tmp():
+def _write_graph_tmp(spec):
     import tempfile
     d = tempfile.mkdtemp(prefix="pticm_bench_")
-    return _graph().write_gset(os.path.join(d, "c2"))   # no extension: 1-based like Gset
+    return _graph(spec).write_gset(os.path.join(d, spec["fname"]))   # c2: no extension, 1-based like Gset
 
 
-def cpu_baseline(pts=400):
-    """Oracle port on one core: about 10 s of CPU work."""
-    path = _write_graph_tmp()
-    sec = _cpu_sample((1, pts, path))
-    attempts = 2 * NT * N_SPINS * pts
+def cpu_baseline(spec, pts=300):
+    """Oracle port on one core, timed over `pts` PT steps after CPU_WARM_PTS."""
+    path = _write_graph_tmp(spec)
+    sec = _cpu_sample((1, 0, pts, path, spec["nt"], spec["T0"], spec["T1"]))
+    attempts = 2 * spec["nt"] * spec["n"] * pts
     return {"value": attempts / sec, "unit": METRIC, "cores": 1, "kind": "port",
-            "sample": f"{pts} PT steps of the workload (ICM on), one process, {sec:.2f} s"}
+            "sample": f"PT steps {CPU_WARM_PTS}..{CPU_WARM_PTS + pts} of the workload (ICM on; the first "
+                      f"{CPU_WARM_PTS} untimed), one process, {sec:.2f} s timed"}
 
 
-def run_reference(args):
+def run_reference(args, spec):
+    """The reference algorithm's CPU implementation (the C oracle port) on
+    every host core: one single-rank process per core, each running
+    CPU_WARM_PTS + warmup*ref_pts PT steps untimed and then steps*ref_pts
+    timed PT steps (its main loop timed inside the process; problem build
+    and initialisation outside).  A bench step is ref_pts PT steps of every
+    process; the job takes the slowest process's time."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     from oracle import pyoracle as O
     O.build()
-    path = _write_graph_tmp()
+    path = _write_graph_tmp(spec)
     cores = os.cpu_count() or 1
-    pts = args.ref_pts
+    pts = args.ref_pts or spec["ref_pts"]
     ctx = mp.get_context("spawn")
-    times = []
     with ctx.Pool(cores) as pool:
-        for step in range(args.warmup + args.steps):
-            t = time.perf_counter()
-            pool.map(_cpu_sample, [(1000 + step * cores + i, pts, path) for i in range(cores)])
-            dt = time.perf_counter() - t
-            if step >= args.warmup:
-                times.append(dt)
-    total = sum(times)
-    attempts = args.steps * cores * 2 * NT * N_SPINS * pts
+        secs = pool.map(_cpu_sample, [(1000 + i, args.warmup * pts, args.steps * pts, path, spec["nt"], spec["T0"],
+                                       spec["T1"]) for i in range(cores)])
+    total = max(secs)
+    attempts = args.steps * cores * 2 * spec["nt"] * spec["n"] * pts
     value = attempts / total
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "attempts/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000 * total / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD.replace("1000 PT steps per bench step",
-                                                    f"{pts} PT steps per process per bench step"),
-                       "parallelism": f"{cores} independent single-rank processes"},
+            "config": {"workload": spec["workload"].replace("1000 PT steps per bench step",
+                                                            f"{pts} PT steps per process per bench step"),
+                       "parallelism": f"{cores} independent single-rank processes",
+                       "untimed_pt_steps_per_process": CPU_WARM_PTS + args.warmup * pts},
             "cpu_baseline": {"value": value, "unit": "attempts/s", "cores": cores, "kind": "port",
-                             "sample": f"{cores} processes x {pts} PT steps per bench step"},
+                             "sample": f"{cores} processes x {args.steps * pts} timed PT steps after "
+                                       f"{CPU_WARM_PTS + args.warmup * pts} untimed ones"},
             "e2e": {"value": value, "unit": "attempts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
 # ---------------------------------------------------------------- GPU leg
-def run_gpu(args):
+def run_gpu(args, spec):
     import numpy as np
     import torch
     import pticm
+    N_SPINS, M_EDGES, NT, T0, T1 = spec["n"], spec["m"], spec["nt"], spec["T0"], spec["T1"]
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -223,7 +242,7 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    inst = _graph()
+    inst = _graph(spec)
     prob = pticm.Problem.from_instance(inst)
     info = prob.info()
     beta = pticm.beta_linspace(T0, T1, NT)
@@ -300,13 +319,17 @@ def run_gpu(args):
     bytes_per_launch = (2 * N_SPINS + 12 * M_EDGES) * 2 * NT * PT_PER_STEP
     launch_s = (sum(dev_ms) / len(dev_ms)) / 1000.0
     achieved = bytes_per_launch / launch_s / 1e9
+    smem_peak = pticm.smem_copy_rate(2000)
+    lay = ctx.layout()
     line = {
         "metric": METRIC, "value": value, "unit": "attempts/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int8 spins, int32 fields/energies",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "l2": "flushed between steps (256 MB write)",
+        "config": {"workload": spec["workload"], "l2": "flushed between steps (256 MB write)",
                    "replicas_per_gpu": 2 * NT, "ncolors": info.ncolors, "icm_pairs": ctx.ladder()[2],
+                   "layout": {"replicas_per_block": lay.replicas_per_block, "blocks": lay.blocks,
+                              "threads": lay.threads, "block_team": lay.block_team},
                    "parallelism": "replicas only" if world > 1 else "1 GPU",
                    "wall_s": wall, "verify_mismatches_after": mism},
         "e2e": {"value": e2e_value, "unit": "attempts/s", "h2d_bytes_per_step": int(h2d),
@@ -315,14 +338,18 @@ def run_gpu(args):
                         "memory + 1000 PT steps + best state/statistics read back, per step"},
         "gpu_launches": args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": _profiled_traffic(),
+                     "frac": achieved / peak, "traffic": _profiled_traffic(spec["profile"]),
                      "note": f"algorithmic bytes 2N+12M per replica-sweep; peak {peak_kind} HBM copy; "
                              "data is shared-memory resident; traffic = ncu DRAM bytes per launch "
-                             "(profiles/pt_engine_c2_bench.md)"},
+                             f"(profiles/{spec['profile']})"},
+        "roofline_smem": {"achieved": achieved, "peak": smem_peak, "unit": "GB/s", "frac": achieved / smem_peak,
+                          "note": "the same algorithmic bytes against the shared-memory copy rate measured in "
+                                  "this run (pticm_smem_copy_rate: one block per SM, read + written bytes), the "
+                                  "tier the replicas and the staged adjacency live in"},
         "clocks": clk.summary(),
     }
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args.cpu_pts)
+        line["cpu_baseline"] = cpu_baseline(spec, args.cpu_pts)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -681,12 +708,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--cpu-pts", type=int, default=400)
-    ap.add_argument("--ref-pts", type=int, default=20)
+    ap.add_argument("--cpu-pts", type=int, default=300)
+    ap.add_argument("--ref-pts", type=int, default=0, help="reference arm: PT steps per process per bench step "
+                    "(0: the workload's default, 20 for c2, 200 for c1)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "batched", "ladder", "large"],
-                    help="c2: the headline single-instance workload; batched: 1024 uneven instances; "
-                         "ladder: the learned temperature ladder; large: N=20000, R=512")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "batched", "ladder", "large"],
+                    help="c2: the headline single-instance workload; c1: the +-J L=20 lattice; batched: 1024 "
+                         "uneven instances; ladder: the learned temperature ladder; large: N=20000, R=512")
     ap.add_argument("--batch-count", type=int, default=BATCH_COUNT)
     ap.add_argument("--ladder-train", type=int, default=4096)
     ap.add_argument("--ladder-held", type=int, default=256)
@@ -700,14 +728,14 @@ def main():
     ap.add_argument("--ttt-target-steps", type=int, default=10000)
     args = ap.parse_args()
     if args.impl == "reference":
-        return run_reference(args)
+        return run_reference(args, SPECS.get(args.workload, SPECS["c2"]))
     if args.workload == "batched":
         return run_gpu_batched(args)
     if args.workload == "ladder":
         return run_gpu_ladder(args)
     if args.workload == "large":
         return run_gpu_large(args)
-    return run_gpu(args)
+    return run_gpu(args, SPECS[args.workload])
 
 
 if __name__ == "__main__":

@@ -554,6 +554,13 @@ PTICM_API int pticm_learned_ladder(const pticm_problem* p, pticm_mlp* m, double 
                                    uint32_t nt, double r, uint64_t check_steps, double tol, uint64_t seed,
                                    double* beta_out, uint32_t* count, pticm_learned_ladder_info* info);
 
+/* The measured shared-memory copy rate of the current GPU (bytes read plus
+ * bytes written per second over all SMs, GB/s): one block per SM copies
+ * between two 96 KB regions of its shared memory `iters` times.  The peak of
+ * the engine's roofline where its data is shared-memory resident.  No
+ * counterpart in the reference. */
+PTICM_API int pticm_smem_copy_rate(int iters, double* gb_per_s);
+
 /* ----------------------------------------------------------- utilities -- */
 PTICM_API const char* pticm_last_error(void);
 PTICM_API const char* pticm_version(void);

@@ -13,6 +13,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 /* ===================================================================== RNG */
 /* Mersenne Twister, 64-bit word size; parameters of std::mt19937_64. */
@@ -710,8 +711,28 @@ static uint64_t walk_ladder(const double* logdos, uint64_t nb, double min_emin, 
                             double beta_start, double beta_end, double step_size, double r,
                             uint64_t num_temps, double* bv);
 
+static double mono_seconds(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+static int solve_impl(orc_problem* p, const orc_params* prm, orc_result* res, uint8_t* best_state,
+                      uint8_t* replica_states, double* final_energy, orc_trace* trace, uint64_t timed_from,
+                      double* timed_s);
+
 int orc_solve(orc_problem* p, const orc_params* prm, orc_result* res,
               uint8_t* best_state, uint8_t* replica_states, double* final_energy, orc_trace* trace) {
+    return solve_impl(p, prm, res, best_state, replica_states, final_energy, trace, UINT64_MAX, NULL);
+}
+
+int orc_solve_timed(orc_problem* p, const orc_params* prm, orc_result* res, uint64_t timed_from, double* timed_s) {
+    return solve_impl(p, prm, res, NULL, NULL, NULL, NULL, timed_from, timed_s);
+}
+
+static int solve_impl(orc_problem* p, const orc_params* prm, orc_result* res, uint8_t* best_state,
+                      uint8_t* replica_states, double* final_energy, orc_trace* trace, uint64_t timed_from,
+                      double* timed_s) {
     memset(res, 0, sizeof(*res));
     pt_t W;
     memset(&W, 0, sizeof(W));
@@ -784,7 +805,9 @@ int orc_solve(orc_problem* p, const orc_params* prm, orc_result* res,
     if (trace) vpush(&trace->off, &zero);
     int rc = 0;
     /* MAIN MCMC LOOP (src/solver.cc:67-127) */
+    double t_from = 0.0;
     for (uint64_t it = 0; it < prm->pts && !rc; it++) {
+        if (it == timed_from) t_from = mono_seconds();
         for (uint64_t sw = 0; sw < prm->sweeps; sw++) {
             for (uint64_t r = 0; r < R; r++) {
                 uint64_t flips, used = 0;
@@ -815,6 +838,7 @@ int orc_solve(orc_problem* p, const orc_params* prm, orc_result* res,
                 if (icm_step(w, (uint64_t)k, t1, t2, tmp, added)) { rc = -3; break; }
         }
     }
+    if (timed_s) *timed_s = timed_from < prm->pts ? mono_seconds() - t_from : 0.0;
     /* gather_best_energy_values (src/mpi_utils.cc:103-163), one rank */
     double best = DBL_MAX;
     uint64_t bsweep = 0;

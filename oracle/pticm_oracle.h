@@ -153,6 +153,11 @@ int64_t orc_overlap(const orc_problem* p, uint8_t* s1, const uint8_t* s2, int64_
  * both states. */
 void orc_bfs_icm(const orc_problem* p, int64_t seed, uint8_t* s1, uint8_t* s2);
 
+/* orc_solve without outputs beyond `res`, timing its main loop from PT step
+ * `timed_from` on: *timed_s receives the wall seconds of steps timed_from ..
+ * pts-1 (the CPU baseline times a run past its random start). */
+int orc_solve_timed(orc_problem* p, const orc_params* prm, orc_result* res, uint64_t timed_from, double* timed_s);
+
 /* ---------------------------------------------- Multihistogram (CAE) ----- */
 /* Restatements of src/cae_estimator.cc: the pilot run (gather_samples :76-151),
  * histograms (:45-69), log-space DOS fixed point (:155-253) and the greedy

@@ -101,6 +101,8 @@ def lib():
         L.orc_trace_copy.argtypes = [P] + [P] * 7
         L.orc_solve.argtypes = [P, C.POINTER(Params), C.POINTER(Result), P, P, P, P]
         L.orc_solve.restype = C.c_int
+        L.orc_solve_timed.argtypes = [P, C.POINTER(Params), C.POINTER(Result), C.c_uint64, P]
+        L.orc_solve_timed.restype = C.c_int
         L.orc_logplusexp2.argtypes = [C.c_double, C.c_double]
         L.orc_logplusexp2.restype = C.c_double
         L.orc_partition_func.argtypes = [P, C.c_uint64, C.c_double, C.c_double, C.c_double]
@@ -306,6 +308,20 @@ def solve(prob: Problem, *, seed, Nt, pts, sweeps=1, T0=0.6, T1=2.8, inverse=Fal
         t["step_energy"] = t["step_energy"][:ne].reshape(-1, R) if ne else np.zeros((0, R))
         out["trace"] = t
     return out
+
+
+def solve_timed(prob: Problem, *, seed, Nt, pts, timed_from, T0=0.6, T1=2.8, icm=False, sweeps=1):
+    """solve() timing its main loop from PT step `timed_from` on: (wall
+    seconds of steps timed_from..pts-1, best energy)."""
+    L = lib()
+    L.orc_mt64_seed(prob.rng(), seed)
+    prm = Params(seed, Nt, pts, sweeps, 2000, 5000, T0, T1, 0.1, 0, 0, int(icm))
+    res = Result()
+    sec = C.c_double()
+    rc = L.orc_solve_timed(prob.h, C.byref(prm), C.byref(res), timed_from, C.byref(sec))
+    if rc:
+        raise RuntimeError(f"oracle solve failed ({rc})")
+    return sec.value, res.best_energy
 
 
 def beta_linspace(T0, T1, nt, inverse=False):

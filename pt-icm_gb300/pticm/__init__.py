@@ -103,6 +103,7 @@ def lib():
         "pticm_icm_pairs": [P, P, u32, C.c_int],
         "pticm_get_exchange_order": [P, P],
         "pticm_get_layout": [P, C.POINTER(Layout)],
+        "pticm_smem_copy_rate": [C.c_int, P],
         "pticm_set_wait_limit": [P, u64, u32],
         "pticm_philox_probe": [P, P, P, C.c_int],
         "pticm_set_profiling": [P, C.c_int],
@@ -279,6 +280,13 @@ def cae_walk(logdos, min_emin, estep, beta_start, beta_end, step_size, r, num_te
     _check(lib().pticm_cae_walk(_p(d), len(d), min_emin, estep, beta_start, beta_end, step_size, r, num_temps,
                                 _p(out), C.byref(cnt)))
     return out[:cnt.value]
+
+
+def smem_copy_rate(iters=2000) -> float:
+    """Measured shared-memory copy rate of the GPU (read + written GB/s)."""
+    r = C.c_double()
+    _check(lib().pticm_smem_copy_rate(iters, C.byref(r)))
+    return r.value
 
 
 def beta_linspace(T0, T1, nt, inverse=False):

@@ -26,7 +26,7 @@ NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=
            "--expt-relaxed-constexpr"] + ARCH
 INCS = ["-I", os.path.join(REPO, "include"), "-I", CSRC]
 
-LIB_SOURCES = ["pt_engine.cu", "runtime.cu", "problem_host.cc", "noalloc.cu", "replica.cu", "mhist.cu", "mhist_host.cc", "tc_gemm.cu", "mlp.cu", "batch.cu", "surrogate.cu"]
+LIB_SOURCES = ["pt_engine.cu", "runtime.cu", "problem_host.cc", "noalloc.cu", "replica.cu", "smem_rate.cu", "mhist.cu", "mhist_host.cc", "tc_gemm.cu", "mlp.cu", "batch.cu", "surrogate.cu"]
 
 
 def nvcc() -> str:

@@ -555,15 +555,19 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                         if (threadIdx.x == 0) P.subtick(PROF_UF_COMPRESS);
                     }
                 }
-                if (team.tr < 32) {
-                    // vote over 32 sampled overlap sites (one warp): a block
-                    // team samples its overlap list; in a warp team each lane
-                    // takes the first overlap site in a 32-byte window of the
-                    // flags (eight independent word loads; the flags start on
-                    // 16 bytes, bytes from n on are masked)
+                int L = -1;
+                if (BLOCK || team.tr < 32) {
+                    // vote over 32 sampled overlap sites: a block team samples
+                    // its overlap list, every warp the same 32 entries, so
+                    // that each warp knows the winner without a barrier (the
+                    // roots do not change until the next union); in a warp
+                    // team each lane takes the first overlap site in a
+                    // 32-byte window of the flags (eight independent word
+                    // loads; the flags start on 16 bytes, bytes from n on are
+                    // masked)
                     int cand = -1;
                     if (BLOCK) {
-                        cand = uf_find(vl, lst[l0 + (int)(((long long)team.tr * llen) >> 5)]);
+                        cand = uf_find(vl, lst[l0 + (int)(((long long)(threadIdx.x & 31) * llen) >> 5)]);
                     } else {
                         const int w0 = (int)(((long long)team.tr * n) >> 7);
                         uint32_t fw[8];
@@ -583,11 +587,14 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                         const int oc = __shfl_xor_sync(0xffffffffu, best, o);
                         if (ov > votes || (ov == votes && oc < best)) { votes = ov; best = oc; }
                     }
-                    if (team.tr == 0) team.ctl[0] = best;
+                    if (BLOCK) L = best;
+                    else if (team.tr == 0) team.ctl[0] = best;
                 }
-                team.sync();
+                if (!BLOCK) {
+                    team.sync();
+                    L = *(volatile int*)team.ctl;
+                }
                 if (threadIdx.x == 0) P.subtick(PROF_UF_VOTE);
-                const int L = *(volatile int*)team.ctl;
                 for_overlap([&](int u) {
                     if (uf_find(vl, u) == L) return;
                     if (BLOCK) {
@@ -638,6 +645,10 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                     unsigned long long m1 = ~0ull, m2 = ~0ull;
                     long long none = 0;
                     team.reduce(c, m1, m2, none);
+                    // every thread has read the list counters: reset them
+                    // for the next pair (a barrier of this pair's flip or
+                    // energy reduction comes before its next use)
+                    if (team.tr == 0) { team.ctl[2] = 0; team.ctl[3] = 0; team.ctl[4] = 0; }
                     csize = (rs == rL) ? cnt - c : c;
                     const bool sw = !exact && csize * 2 > cnt;
                     fast = (rs == rL) ? sw : !sw;   // the flipped set lies in S
@@ -813,12 +824,16 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
             if (locB && cnt > 0) B.E[rB] += dEb;
         }
     }
-    if (BLOCK && team.tr == 0) {
-        team.ctl[2] = 0;   // the list counters, for the next pair
-        team.ctl[3] = 0;
-        team.ctl[4] = 0;
+    if (!(BLOCK && algo == ENGINE_ICM_UNION_FIND && cnt > 0)) {
+        // (a block team's union-find reset the list counters after its size
+        // reduction and passed a barrier since)
+        if (BLOCK && team.tr == 0) {
+            team.ctl[2] = 0;   // the list counters, for the next pair
+            team.ctl[3] = 0;
+            team.ctl[4] = 0;
+        }
+        team.sync();
     }
-    team.sync();
     if (threadIdx.x == 0) {
         P.subtick(PROF_ICM_FLIP);
         if (P.on && cnt > 0) P.c[PROF_ICM_COUNT]++;

@@ -370,11 +370,26 @@ def run_gpu_batched(args):
     import pticm
     from pticm import instances as I
 
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from pticm import sharding as SH
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
     t_gen = time.perf_counter()
-    insts = I.batch_mix(args.batch_count)
+    all_insts = I.batch_mix(args.batch_count)
+    # N GPUs: the instances are split by cost (pticm.sharding), each rank runs
+    # its share as a batch of its own; nothing crosses GPUs while it runs
+    costs = [SH.instance_cost(x.n, x.m, 2 * BATCH_NT) for x in all_insts]
+    share = SH.partition(costs, world)[rank]
+    insts = [all_insts[i] for i in share]
     probs = [pticm.Problem.from_instance(x) for x in insts]
     t_gen = time.perf_counter() - t_gen
+    total_sites = sum(x.n for x in all_insts) * 2 * BATCH_NT
     beta = pticm.beta_linspace(0.5, 3.0, BATCH_NT)
     bat = pticm.Batch(probs, nt=BATCH_NT, seed=1, icm=True, exchange=1)
     bat.set_ladders(beta)
@@ -391,19 +406,26 @@ def run_gpu_batched(args):
         raise RuntimeError("verify found mismatches after warm-up")
     dev_ms = []
     launches0 = bat.info().launches
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    barrier()
     wall0 = time.perf_counter()
-    with ClockSampler(0) as clk:
+    with ClockSampler(local) as clk:
         for _ in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
             bat.run(BATCH_PT_PER_STEP)
             dev_ms.append(bat.info().last_run_ms)
+    barrier()
     launches = bat.info().launches - launches0
-    torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     info = bat.info()
-    total_ms = sum(dev_ms)
-    value = sites * BATCH_PT_PER_STEP * args.steps / (total_ms / 1000.0)
+    total_ms = max_over_ranks(sum(dev_ms), dist, "cuda")
+    value = total_sites * BATCH_PT_PER_STEP * args.steps / (total_ms / 1000.0)
     mism = bat.verify()
     g, t_us, staged, teams = bat.groups()
     # end to end: problems from host edge lists, ladders, states, the run and
@@ -415,7 +437,7 @@ def run_gpu_batched(args):
     import concurrent.futures as cf
     pool = cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 1)
     for i in range(args.e2e_steps):
-        torch.cuda.synchronize()
+        barrier()
         t0 = time.perf_counter()
         ps = list(pool.map(lambda x: pticm.Problem.from_coo(x.n, x.src, x.dst, x.w), insts))
         b2 = pticm.Batch(ps, nt=BATCH_NT, seed=50 + i, icm=True, exchange=1)
@@ -424,25 +446,34 @@ def run_gpu_batched(args):
         b2.run(BATCH_PT_PER_STEP)
         best, flips = b2.best()
         del b2, ps
-        torch.cuda.synchronize()
-        e2e_t.append(time.perf_counter() - t0)
+        barrier()
+        e2e_t.append(max_over_ranks(time.perf_counter() - t0, dist, "cuda"))
+    # the per-instance results of every rank, gathered after the timed runs
+    results = SH.gather_results({i: (float(e), int(f)) for i, e, f in zip(share, *bat.best())}, world, dist)
+    if rank != 0:
+        dist.destroy_process_group()
+        return 0
+    if len(results) != len(all_insts):
+        raise RuntimeError("sharded run lost instances")
     peak, peak_kind = _peaks()
-    launch_s = total_ms / 1000.0 / args.steps
+    launch_s = sum(dev_ms) / 1000.0 / args.steps   # this rank's launches and its share's bytes
     achieved = bytes_per_sweep * BATCH_PT_PER_STEP / launch_s / 1e9
     line = {
-        "metric": METRIC, "value": value, "unit": "attempts/s", "n_gpus": 1, "steps": args.steps,
+        "metric": METRIC, "value": value, "unit": "attempts/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "int8 spins, int32 fields/energies", "data": "synthetic",
+        "scaling": "strong", "vs_baseline": None, "dtype": "int8 spins, int32 fields/energies", "data": "synthetic",
         "config": {"workload": BATCH_WORKLOAD if args.batch_count == BATCH_COUNT else
                    BATCH_WORKLOAD.replace("1024 uneven", f"{args.batch_count} uneven"),
-                   "instances": len(insts), "sites_per_sweep": sites,
+                   "instances": len(all_insts), "instances_rank0": len(insts), "sites_per_sweep": total_sites,
+                   "parallelism": f"instances split over {world} GPUs by cost (replicas only)" if world > 1
+                   else "1 GPU",
                    "l2": "flushed between steps (256 MB write); the working set also exceeds L2",
                    "lanes": info.lanes, "jobs": info.jobs, "chunk_pt_steps": info.chunk, "smem_bytes": info.smem_bytes,
                    "predicted_makespan_us_per_pt_step": info.makespan_us,
                    "groups": {str(k): int(v) for k, v in zip(*np.unique(g, return_counts=True))},
                    "staged_instances": int(staged.sum()), "autotune_s": t_tune, "generate_s": t_gen,
                    "wall_s": wall, "verify_mismatches_after": mism},
-        "e2e": {"value": sites * BATCH_PT_PER_STEP / statistics.median(e2e_t), "unit": "attempts/s",
+        "e2e": {"value": total_sites * BATCH_PT_PER_STEP / statistics.median(e2e_t), "unit": "attempts/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 16 * len(insts),
                 "what": "all problems from host edge lists (colouring on all host cores) + ladders + states + "
                         "100 PT steps + per-instance best energies back"},
@@ -453,6 +484,8 @@ def run_gpu_batched(args):
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
     return 0
 
 

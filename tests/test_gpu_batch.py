@@ -167,3 +167,26 @@ def test_batch_logdos_matches_oracle():
         shift = np.median(dos_g[filled] - dos_o[filled])
         assert np.allclose(dos_g[filled] - shift, dos_o[filled], rtol=0,
                            atol=2e-3 * max(1.0, np.abs(dos_o[filled]).max()))
+
+
+def test_instance_shares_run_as_separate_batches():
+    """The shares of a sharded batch (pticm.sharding: three ranks' worth, run
+    one after another on this GPU) each run as a batch of their own: every
+    instance is run once, fields and energies stay exact, and every instance
+    reaches a best energy."""
+    import pticm
+    from pticm import instances as I
+    from pticm import sharding as S
+    insts = I.batch_mix(24, seed0=4000)
+    probs = [pticm.Problem.from_instance(x) for x in insts]
+    costs = [S.instance_cost(x.n, x.m, 2 * 8) for x in insts]
+    shares = S.partition(costs, 3)
+    merged = {}
+    for rank, share in enumerate(shares):
+        res, bat = S.run_shard(probs, share, nt=8, seed=10 + rank, steps=30, autotune_steps=0)
+        assert bat.verify() == 0
+        assert set(res) == set(share)
+        merged.update(res)
+    assert sorted(merged) == list(range(len(insts)))
+    assert all(e < 0 for e, _ in merged.values())
+    assert all(f > 0 for _, f in merged.values())

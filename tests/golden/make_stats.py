@@ -21,6 +21,9 @@ Configurations:
   rnd200_w1   random N=200 graph, w=+1, 10 temperatures T 0.5..15, ICM
   rnd1000_pm  random N=1000, M=5000 graph, +-1, 24 temperatures T 0.5..5, ICM
   c2          random N=2000, M=19990 graph, w=+1, 64 temperatures T 0.5..15, ICM (the C2 shape)
+  c5_hot      the C5 graph (N=20000, M=400000, +-1), 6 temperatures T 6..9.5: the paramagnetic end of
+              the C5 ladder, run in the large-instance layout (its ICM temperatures, T <= 1, lie deep
+              in the glass phase and do not equilibrate in reach of the oracle)
 
     python tests/golden/make_stats.py [name ...] [--procs P]
 """
@@ -46,14 +49,15 @@ CONFIGS = {
     "rnd200_w1": dict(graph="rnd200_w1", nt=10, T0=0.5, T1=15.0, pts=8000, burn=4000),
     "rnd1000_pm": dict(graph="rnd1000_pm", nt=24, T0=0.5, T1=5.0, pts=16000, burn=8000),
     "c2": dict(graph="c2", nt=64, T0=0.5, T1=15.0, pts=64000, burn=32000),
+    "c5_hot": dict(graph="c5", nt=6, T0=6.0, T1=9.5, pts=4000, burn=2000),
 }
 
 
 def graph_path(name, scratch):
-    """Committed golden graphs, or the seeded C2 instance written to `scratch`."""
-    if name == "c2":
+    """Committed golden graphs, or the seeded C2 / C5 instances written to `scratch`."""
+    if name in ("c2", "c5"):
         from pticm import instances
-        return instances.c2().write_gset(os.path.join(scratch, "c2"))   # 1-based, like Gset
+        return getattr(instances, name)().write_gset(os.path.join(scratch, name))   # 1-based, like Gset
     return os.path.join(HERE, "graphs", name)
 
 

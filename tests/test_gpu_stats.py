@@ -116,9 +116,10 @@ def _fixture(name):
 
 def _fixture_graph(name, fx, tmp_path):
     import hashlib
-    if name == "c2":
+    if name in ("c2", "c5_hot"):
         from pticm import instances
-        path = instances.c2().write_gset(str(tmp_path / "c2"))
+        g = fx["config"]["graph"]
+        path = getattr(instances, g)().write_gset(str(tmp_path / g))
     else:
         path = os.path.join(G, fx["config"]["graph"])
     with open(path, "rb") as f:
@@ -154,16 +155,19 @@ def _gpu_block_runs(path, c, seeds, exchange, rpb):
 
 @pytest.mark.parametrize("exchange", [1, 0])
 @pytest.mark.parametrize("name,rpb", [("pmL20_c1", 1), ("pmL20_c1", 8), ("rnd200_w1", 1), ("rnd200_w1", 4),
-                                      ("rnd1000_pm", 1), ("rnd1000_pm", 4), ("c2", 1)])
+                                      ("rnd1000_pm", 1), ("rnd1000_pm", 4), ("c2", 1), ("c5_hot", 1)])
 def test_block_layouts_match_oracle_statistics(name, rpb, exchange, tmp_path):
     fx = _fixture(name)
     c = fx["config"]
     path = _fixture_graph(name, fx, tmp_path)
     gm, grate, nc, lay, gbest = _gpu_block_runs(path, c, 16, exchange, rpb)
-    assert nc == fx["nc"] > 0, "ICM pairs differ from the reference's count"
+    assert nc == fx["nc"], "ICM pairs differ from the reference's count"
+    assert nc > 0 or name == "c5_hot"
     assert lay.replicas_per_block == rpb
     if rpb == 1:
         assert lay.block_team == 1, "one replica per block runs the block-team kernel"
+    if name == "c5_hot":
+        assert lay.state_mode == 1, "the C5 graph runs in the large-instance layout (fields gathered)"
     om = np.array(fx["mean_energy"])
     orate = np.array(fx["acceptance"])
     # equilibrium temperatures: the reference algorithm's mean energies over
@@ -181,8 +185,10 @@ def test_block_layouts_match_oracle_statistics(name, rpb, exchange, tmp_path):
     # acceptance there is compared only in the reference's own order.
     if not (name == "c2" and exchange == 1):
         z = np.concatenate([z, _agree(grate[:, eq_pairs], orate[:, eq_pairs])])
-    # the best energy of the reference algorithm's runs is reached
-    assert gbest.min() <= min(fx["best_energy"]), (gbest, fx["best_energy"])
+    # the best energy of the reference algorithm's runs is reached (not at the
+    # paramagnetic end of C5, where the best is a chance low of hot states)
+    if name != "c5_hot":
+        assert gbest.min() <= min(fx["best_energy"]), (gbest, fx["best_energy"])
     allowed = max(1, math.ceil(0.02 * len(z)))
     assert (z > 3.0).sum() <= allowed, (np.round(z, 2), allowed)
     assert z.max() < 4.5, np.round(z, 2)

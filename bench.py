@@ -490,8 +490,8 @@ def run_gpu_batched(args):
 
 
 LARGE_WORKLOAD = ("random +-1 MaxCut graph N=20000, mean degree 40 (M=400000, seed 5), 128 temperatures linear "
-                  "in beta for T 0.5..9.5 x 4 replicas per temperature (R=512), ICM on; replicas, adjacency and ICM "
-                  "scratch in device memory (L2-resident); 20 PT steps per bench step")
+                  "in beta for T 0.5..9.5 x 4 replicas per temperature, ICM on; spins in shared memory, fields "
+                  "gathered at each visit, adjacency and ICM scratch in device memory; 20 PT steps per bench step")
 
 
 def run_gpu_large(args):
@@ -500,12 +500,32 @@ def run_gpu_large(args):
     import pticm
     from pticm import instances as I
 
+    from pticm import surrogate as S
+
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     inst = I.c5()
     prob = pticm.Problem.from_instance(inst)
     info = prob.info()
-    ctx = pticm.Context(prob, nt=128, chains=4, seed=1, icm=True)
-    ctx.set_ladder(pticm.beta_linspace(0.5, 9.5, 128))
+    # the ladder: 128 temperatures from the surrogate network, checked by a
+    # short PT run, with the multihistogram ladder as fallback (the learned
+    # ladder); ascending in beta, so that ICM takes the coldest slots
+    t_lad = time.perf_counter()
+    lad_info = None
+    if args.large_ladder == "linear":
+        beta = pticm.beta_linspace(0.5, 9.5, 128)
+    else:
+        if args.ladder_net:
+            net = S.load(args.ladder_net)
+        else:
+            recs = S.make_records(I.ladder_mix(args.large_train, seed0=100), nt=32, burn_in=1000, samples=2000,
+                                  seed=3)
+            net, _ = S.train(recs, steps=3000, batch=1024, lr=1e-3, seed=1)
+        beta, lad_info = S.learned_ladder(prob, net, 0.5, 9.5, 128, seed=21)
+        beta = np.sort(np.asarray(beta, np.float64))
+    t_lad = time.perf_counter() - t_lad
+    NTL = len(beta)
+    ctx = pticm.Context(prob, nt=NTL, chains=4, seed=1, icm=True)
+    ctx.set_ladder(beta)
     ctx.init_states(2)
     steps_per = 20
     for _ in range(args.warmup):
@@ -518,14 +538,13 @@ def run_gpu_large(args):
             ctx.run(steps_per)
             dev_ms.append(ctx.stats()[0].last_run_ms)
     total_ms = sum(dev_ms)
-    sites = 512 * inst.n
+    sites = 4 * NTL * inst.n
     value = sites * steps_per * args.steps / (total_ms / 1000.0)
     mism = ctx.verify()
     # end to end from host buffers: the problem from its edge list, the
     # ladder, the warmed-up replicas as initial states (each to the replica
     # that starts at its temperature), 100 PT steps, best state and
     # statistics back
-    beta = pticm.beta_linspace(0.5, 9.5, 128)
     s_now, _, _, slot_now = ctx.replicas()
     by_slot = np.empty_like(s_now)
     by_slot[slot_now] = s_now
@@ -541,7 +560,7 @@ def run_gpu_large(args):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         p2 = pticm.Problem.from_coo(inst.n, src, dst, w)
-        c2 = pticm.Context(p2, nt=128, chains=4, seed=100 + i, icm=True)
+        c2 = pticm.Context(p2, nt=NTL, chains=4, seed=100 + i, icm=True)
         c2.set_ladder(beta)
         c2.set_states(states_host.numpy())
         c2.run(e2e_pt)
@@ -553,14 +572,29 @@ def run_gpu_large(args):
         if i > 0:
             e2e_t.append(time.perf_counter() - t0)
     peak, peak_kind = _peaks()
-    bytes_per_sweep = (2 * inst.n + 12 * inst.m) * 512
+    bytes_per_sweep = (2 * inst.n + 12 * inst.m) * 4 * NTL
     achieved = bytes_per_sweep * steps_per / (total_ms / 1000.0 / args.steps) / 1e9
+    lay = ctx.layout()
+    workload = LARGE_WORKLOAD if args.large_ladder == "linear" else LARGE_WORKLOAD.replace(
+        "128 temperatures linear in beta for T 0.5..9.5", f"{NTL} temperatures of the learned ladder for T 0.5..9.5")
     line = {"metric": METRIC, "value": value, "unit": "attempts/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int8 spins, int32 fields/energies",
-            "data": "synthetic", "config": {"workload": LARGE_WORKLOAD, "ncolors": info.ncolors,
+            "data": "synthetic", "config": {"workload": workload, "ncolors": info.ncolors,
                                             "icm_pairs": int(ctx.ladder()[2]), "verify_mismatches_after": mism,
-                                            "l2": "the working set (about 170 MB) exceeds L2"},
+                                            "l2": "the working set (about 170 MB) exceeds L2",
+                                            "layout": {"replicas_per_block": lay.replicas_per_block,
+                                                       "blocks": lay.blocks, "threads": lay.threads,
+                                                       "state_mode": lay.state_mode},
+                                            "ladder": {"kind": args.large_ladder, "temperatures": NTL,
+                                                       "beta_min": float(beta.min()), "beta_max": float(beta.max()),
+                                                       "setup_s": t_lad,
+                                                       "fallback": None if lad_info is None else int(lad_info.fallback),
+                                                       "checks": None if lad_info is None else int(lad_info.rounds),
+                                                       "mean_abs_acceptance_deviation": None if lad_info is None
+                                                       else float(lad_info.mean_deviation),
+                                                       "network": args.ladder_net or
+                                                       f"trained in this run on {args.large_train} pilot instances"}},
             "e2e": {"value": sites * e2e_pt / statistics.median(e2e_t), "unit": "attempts/s",
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "what": f"problem from its edge list (colouring on the host) + ladder + the warmed-up replicas "
@@ -579,6 +613,24 @@ LADDER_WORKLOAD = ("learned ladder: 4x256 SiLU MLP (BF16 weights, FP32 accumulat
                    "trained on FP64 multihistogram ln g of synthetic instances (+-J lattices L 6..50, +-1 random "
                    "graphs N 100..3000, mean degree 3..20); evaluated on held-out instances: ln g error, ladder "
                    "acceptance (r=0.4, 32 temperatures), ladder cost and time-to-target vs the multihistogram ladder")
+
+
+def _tmpdir():
+    import tempfile
+    global _TMP
+    try:
+        return _TMP
+    except NameError:
+        _TMP = tempfile.mkdtemp(prefix="pticm_bench_")
+        return _TMP
+
+
+def _gset_digest(inst, fname):
+    """SHA-256 of the instance written in Gset layout (1-based, no extension)."""
+    import hashlib
+    path = inst.write_gset(os.path.join(_tmpdir(), fname))
+    with open(path, "rb") as f:
+        return hashlib.sha256(f.read()).hexdigest()
 
 
 def _ttt_runs(prob, ladder, target, copies, chunk, max_steps, seed):
@@ -652,6 +704,14 @@ def run_gpu_ladder(args):
     col = lambda k: np.array([q[k] for q in rows], np.float64)
     # time to target on a subset of held-out instances
     ttt = []
+    targets = {}
+    tpath = os.path.join(ROOT, "tests", "golden", "ttt_targets.json")
+    if os.path.exists(tpath) and args.ladder_held == 256:
+        with open(tpath) as f:
+            for d in json.load(f)["instances"]:
+                # the instance the oracle ran (same generator output, same file)
+                if _gset_digest(held[d["index"]], f"t{d['index']}") == d["graph_sha256"]:
+                    targets[d["index"]] = d["target"]
     cand = [i for i, x in enumerate(held) if args.ttt_min_n <= x.n <= args.ttt_max_n][:args.ttt_count]
     for i in cand:
         x = held[i]
@@ -666,14 +726,19 @@ def run_gpu_ladder(args):
         t = time.perf_counter()
         bs = S.surrogate_ladder(p, m, T0, T1, 32)
         t_s = time.perf_counter() - t
-        # target: best energy of a long multihistogram-laddered run, 32 copies
-        tb = pticm.Batch([p] * 32, nt=len(bm), seed=80 + i, icm=True, exchange=1)
-        tb.set_ladders(np.sort(bm))
-        tb.init_states(81 + i)
-        tb.run(args.ttt_target_steps)
-        target = float(tb.best()[0].min())
-        del tb
-        res = {"n": x.n, "name": x.name, "target": target}
+        # target: the best energy the reference algorithm reached (the C oracle,
+        # four long runs on its linear ladder; tests/golden/ttt_targets.json),
+        # else the best of a long multihistogram-laddered run of 32 copies
+        if i in targets:
+            target, tsrc = targets[i], "reference algorithm (oracle), best of 4 x 10000 PT steps"
+        else:
+            tb = pticm.Batch([p] * 32, nt=len(bm), seed=80 + i, icm=True, exchange=1)
+            tb.set_ladders(np.sort(bm))
+            tb.init_states(81 + i)
+            tb.run(args.ttt_target_steps)
+            target, tsrc = float(tb.best()[0].min()), "32 copies of a multihistogram-laddered GPU run"
+            del tb
+        res = {"n": x.n, "name": x.name, "target": target, "target_source": tsrc}
         for nm, lad, tl in (("mhist", bm, t_m), ("learned", bl, t_l), ("surrogate", bs, t_s)):
             hit, msps = _ttt_runs(p, lad, target, args.ttt_copies, args.ttt_chunk, args.ttt_max_steps, 90 + i)
             ok = hit >= 0
@@ -749,12 +814,18 @@ def main():
                     help="c2: the headline single-instance workload; c1: the +-J L=20 lattice; batched: 1024 "
                          "uneven instances; ladder: the learned temperature ladder; large: N=20000, R=512")
     ap.add_argument("--batch-count", type=int, default=BATCH_COUNT)
+    ap.add_argument("--large-ladder", default="learned", choices=["learned", "linear"],
+                    help="large workload: the learned ladder (surrogate + checks + multihistogram fallback, the "
+                         "workload's definition) or 128 temperatures linear in beta")
+    ap.add_argument("--large-train", type=int, default=1024,
+                    help="large workload: pilot instances the in-run surrogate network trains on")
+    ap.add_argument("--ladder-net", default="", help="a saved surrogate network (pticm_mlp_save) to use instead")
     ap.add_argument("--ladder-train", type=int, default=4096)
     ap.add_argument("--ladder-held", type=int, default=256)
     ap.add_argument("--ladder-eval", type=int, default=64)
-    ap.add_argument("--ttt-count", type=int, default=8)
+    ap.add_argument("--ttt-count", type=int, default=32)
     ap.add_argument("--ttt-min-n", type=int, default=200)
-    ap.add_argument("--ttt-max-n", type=int, default=1500)
+    ap.add_argument("--ttt-max-n", type=int, default=3000)
     ap.add_argument("--ttt-copies", type=int, default=100)
     ap.add_argument("--ttt-chunk", type=int, default=50)
     ap.add_argument("--ttt-max-steps", type=int, default=10000)

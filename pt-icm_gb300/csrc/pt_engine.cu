@@ -167,6 +167,7 @@ struct IcmScratch {
     uint8_t* d;
     uint32_t* vis;
     int* list;          // block team only: overlap sites first, the others from the end
+    int* link1;         // (device-memory list only) each list site's second overlap neighbour, or null
 };
 
 __device__ __forceinline__ IcmScratch icm_scratch(uint8_t* base, int n_pad) {
@@ -175,6 +176,7 @@ __device__ __forceinline__ IcmScratch icm_scratch(uint8_t* base, int n_pad) {
     X.d = base + (size_t)n_pad * 4;
     X.vis = reinterpret_cast<uint32_t*>(base + (size_t)n_pad * 5);
     X.list = reinterpret_cast<int*>(base + icm_team_bytes(n_pad));
+    X.link1 = nullptr;
     return X;
 }
 
@@ -218,7 +220,7 @@ __device__ __forceinline__ void for_each_neighbour(const int32_t* row, const uin
 // the set (s_v equal in A and B), an exact integer update.  Members held by
 // another block are read from the published copy and flipped by their own
 // block, which finds the same set.
-template <bool BLOCK, bool REPLAY, bool LS>
+template <bool BLOCK, bool REPLAY, bool LS, bool GLINK = false>
 __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK>& team, int q,
                          int rA, int rB, unsigned long long step, int ls, const IcmScratch& X,
                          int where_err, Prof& P) {
@@ -522,7 +524,81 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                 // full adjacency only of sites outside L.  An edge skipped at
                 // an end in L is processed from its other end, unless that end
                 // is in L too -- then both are already joined.
+                // (GLINK: with the neighbour lists in device memory, a
+                // thread scans four of its sites side by side, so that
+                // their dependent loads overlap, then makes their unions)
+                const bool glink = GLINK && BLOCK && !__isShared(B.adj);
+                // (round 0 also finds each site's second overlap neighbour
+                // and keeps it, by list position, for round 1)
+                int* const link1 = glink ? X.link1 : nullptr;
                 for (int round = 0; round < 2; round++) {
+                    if (glink && round == 1 && link1 != nullptr) {
+                        for (int t = team.tr; t < llen; t += 4 * team.ts) {
+                            int u[4], tg[4];
+#pragma unroll
+                            for (int k = 0; k < 4; k++) {
+                                const int tk = t + k * team.ts;
+                                u[k] = tk < llen ? lst[l0 + tk] : -1;
+                                tg[k] = tk < llen ? link1[tk] : -1;
+                            }
+#pragma unroll
+                            for (int k = 0; k < 4; k++)
+                                if (u[k] >= 0 && tg[k] >= 0) ok &= uf_unite(lab, u[k], tg[k]);
+                        }
+                    } else if (glink) {
+                        for (int t = team.tr; t < llen; t += 4 * team.ts) {
+                            int u[4], a[4], e[4], tg[4], k4[4];
+#pragma unroll
+                            for (int k = 0; k < 4; k++) {
+                                const int tk = t + k * team.ts;
+                                u[k] = tk < llen ? lst[l0 + tk] : -1;
+                            }
+#pragma unroll
+                            for (int k = 0; k < 4; k++) {
+                                a[k] = u[k] >= 0 ? B.row[u[k]] : 0;
+                                e[k] = u[k] >= 0 ? B.row[u[k] + 1] : 0;
+                            }
+                            uint32_t v[4][4];
+#pragma unroll
+                            for (int k = 0; k < 4; k++)
+#pragma unroll
+                                for (int j = 0; j < 4; j++) v[k][j] = a[k] + j < e[k] ? B.adj[a[k] + j] : 0xFFFFFFFFu;
+                            // the round-th overlap neighbour (tg) and, in
+                            // round 0 with a place to keep it, the next (t1)
+                            const int want = (round == 0 && link1 != nullptr) ? 2 : round + 1;
+                            int t1[4];
+#pragma unroll
+                            for (int k = 0; k < 4; k++) {
+                                tg[k] = -1;
+                                t1[k] = -1;
+                                k4[k] = 0;
+#pragma unroll
+                                for (int j = 0; j < 4; j++) {
+                                    const bool on = v[k][j] != 0xFFFFFFFFu && d[v[k][j] >> 8];
+                                    if (on && k4[k] < want) {
+                                        if (k4[k] == round) tg[k] = (int)(v[k][j] >> 8);
+                                        else if (k4[k] == round + 1) t1[k] = (int)(v[k][j] >> 8);
+                                        k4[k]++;
+                                    }
+                                }
+                            }
+#pragma unroll
+                            for (int k = 0; k < 4; k++) {
+                                if (u[k] < 0) continue;
+                                // rarely: the targets lie past the first four entries
+                                for (int aa = a[k] + 4; aa < e[k] && k4[k] < want; aa++) {
+                                    const int w = (int)(B.adj[aa] >> 8);
+                                    if (d[w]) {
+                                        if (k4[k] == round) tg[k] = w;
+                                        else if (k4[k] == round + 1) t1[k] = w;
+                                        k4[k]++;
+                                    }
+                                }
+                                if (round == 0 && link1 != nullptr) link1[t + k * team.ts] = t1[k];
+                                if (tg[k] >= 0) ok &= uf_unite(lab, u[k], tg[k]);
+                            }
+                        }
+                    } else
                     for_overlap([&](int u) {
                         // the neighbour list four entries at a time: four
                         // independent loads, then four flag loads
@@ -546,6 +622,24 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                     if (round == 0) {
                         // (after the last round the vote's and phase 3's
                         // finds halve the paths they walk)
+                        if (glink) {
+                            // four list entries loaded side by side
+                            for (int t = team.tr; t < llen; t += 4 * team.ts) {
+                                int u[4];
+#pragma unroll
+                                for (int k = 0; k < 4; k++) {
+                                    const int tk = t + k * team.ts;
+                                    u[k] = tk < llen ? lst[l0 + tk] : -1;
+                                }
+#pragma unroll
+                                for (int k = 0; k < 4; k++) {
+                                    if (u[k] < 0) continue;
+                                    const int r = uf_find(vl, u[k]);
+                                    if (r < 0) ok = false;
+                                    else vl[u[k]] = r;
+                                }
+                            }
+                        } else
                         for_overlap([&](int u) {
                             const int r = uf_find(vl, u);
                             if (r < 0) ok = false;
@@ -855,6 +949,9 @@ __device__ __forceinline__ int gather_field(const int32_t* row, const uint32_t* 
 // (on C2, 4 to 8 measured best: 26.5 us per PT step against 27.6 with every
 // lane pushing its own).
 constexpr int kCoopPushSites = 4;
+// With fields gathered and several replicas in a block, a thread visits one
+// site of each of at most this many replicas per neighbour-list read.
+constexpr int kGatherReps = 4;
 
 // Colour-class Metropolis sweep of the block's replicas (production).
 // dE_i = -2 s_i (h_i + f_i); accepted with probability min(1, exp(-beta dE))
@@ -880,6 +977,8 @@ __device__ void colored_sweep(const EngineArgs& A, const BlockCtx& B, unsigned l
     rng.start(stream_key(A.seed, STREAM_SWEEP), (uint32_t)(B.rank * T + tid), sweep_idx, (uint32_t)D.inst_id << 16);
     int acc_de = 0;
     unsigned acc_fl = 0;
+    // several replicas in the block, fields gathered
+    const bool gm = !ONE && B.field == nullptr && rpc <= kGatherReps;
     for (int c = 0; c < D.ncolors; c++) {
         const int c0 = s_col[c];
         const int Sc = s_col[c + 1] - c0;
@@ -955,6 +1054,79 @@ __device__ void colored_sweep(const EngineArgs& A, const BlockCtx& B, unsigned l
                         const int dl = -2 * s;
                         for_each_neighbour(row, adj, i,
                                            [&](uint32_t e) { atomicAdd(fd + (e >> 8), (int)(int8_t)(e & 0xffu) * dl); });
+                    }
+                }
+            }
+        } else if (gm) {
+            // a thread visits site i of each of the block's replicas: the
+            // neighbour list is read once for all of them (sites of one
+            // colour class share no edge, so the gathered spins are settled)
+            int g_de[kGatherReps];
+            unsigned g_fl[kGatherReps];
+#pragma unroll
+            for (int j = 0; j < kGatherReps; j++) {
+                g_de[j] = 0;
+                g_fl[j] = 0;
+            }
+            for (int i = c0 + tid; i < c0 + Sc; i += T) {
+                int f[kGatherReps];
+#pragma unroll
+                for (int j = 0; j < kGatherReps; j++) f[j] = 0;
+                auto visit = [&](uint32_t e) {
+                    const int w = (int)(int8_t)(e & 0xffu);
+                    const int8_t* sn = B.spin + (e >> 8);
+#pragma unroll
+                    for (int j = 0; j < kGatherReps; j++)
+                        if (j < rpc) f[j] += w * sn[j * npad];
+                };
+                // the neighbour list 16 bytes at a time, one load in flight
+                // (four spin loads per entry keep the thread busy)
+                int a = row[i];
+                const int a1 = row[i + 1];
+                if ((reinterpret_cast<uintptr_t>(adj) & 15u) == 0) {
+                    for (; a < a1 && (a & 3); a++) visit(adj[a]);
+#pragma unroll 1
+                    for (; a + 4 <= a1; a += 4) {
+                        const uint4 q = *reinterpret_cast<const uint4*>(adj + a);
+                        visit(q.x);
+                        visit(q.y);
+                        visit(q.z);
+                        visit(q.w);
+                    }
+                }
+                for (; a < a1; a++) visit(adj[a]);
+                const int hi = D.has_h ? B.h[i] : 0;
+#pragma unroll
+                for (int j = 0; j < kGatherReps; j++) {
+                    if (j < rpc) {
+                        int8_t* sp = B.spin + j * npad;
+                        const int s = sp[i];
+                        const int de = -2 * s * (f[j] + hi);
+                        bool acc = de <= 0;
+                        if (!acc) {
+                            const uint32_t thr = s_thr[B.tb[j] + min(de >> 1, kmax)];
+                            acc = (rng.next() < thr) || (thr == 0xFFFFFFFFu);
+                        }
+                        if (acc) {
+                            sp[i] = (int8_t)-s;
+                            g_de[j] += de;
+                            g_fl[j]++;
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < kGatherReps; j++) {
+                if (j < rpc) {
+                    int v = g_de[j];
+                    unsigned f = g_fl[j];
+                    for (int o = 16; o > 0; o >>= 1) {
+                        v += __shfl_xor_sync(0xffffffffu, v, o);
+                        f += __shfl_xor_sync(0xffffffffu, f, o);
+                    }
+                    if (lane == 0 && (v != 0 || f != 0)) {
+                        atomicAdd(s_dEp + j, v);
+                        atomicAdd(s_flp + j, f);
                     }
                 }
             }
@@ -1344,8 +1516,9 @@ __global__ void __launch_bounds__((REPLAY || (BLOCKTEAM && !NARROW)) ? 1024 : kN
     uint32_t* s_xrand = sm_ptr<uint32_t>(smem, S.xrand);
     int* s_lvl = sm_ptr<int>(smem, S.xlevel);
     uint32_t* s_tmp = sm_ptr<uint32_t>(smem, S.xpos);
-    uint8_t* s_icm = (S.state_global || S.field_gather) ? A.icm_pool + (size_t)blockIdx.x * (size_t)A.icm_pool_stride
-                                                          : smem + S.icm;
+    uint8_t* s_icm = ((S.state_global || S.field_gather) && !S.icm_split)
+                         ? A.icm_pool + (size_t)blockIdx.x * (size_t)A.icm_pool_stride
+                         : smem + S.icm;
     int* s_misc = sm_ptr<int>(smem, S.misc);
     long long* s_mag = sm_ptr<long long>(smem, S.mag);
     long long* s_team_acc = sm_ptr<long long>(smem, S.misc + 64);
@@ -1557,14 +1730,19 @@ __global__ void __launch_bounds__((REPLAY || (BLOCKTEAM && !NARROW)) ? 1024 : kN
             // pair per block-wide team, in sequence, beats a pair per warp)
             if (BLOCKTEAM || D.teams == 1) {
                 const Team<true> team{tid, T, s_team_acc, s_team_bc};
-                const IcmScratch X = icm_scratch(s_icm, npad);
+                IcmScratch X = icm_scratch(s_icm, npad);
+                if (!BLOCKTEAM && !REPLAY && S.icm_split) {
+                    X.list = reinterpret_cast<int*>(A.icm_pool + (size_t)blockIdx.x * (size_t)A.icm_pool_stride);
+                    X.link1 = X.list + npad;
+                }
                 for (int j = 0; j < rpc; j++) {
                     const int sl = (int)B.rslot[j], c = sl / nt, k = sl - c * nt, kk = nt - 1 - k;
                     if (kk >= D.nc || c >= chains_even) continue;
                     const int cp = c >> 1;
                     const int rA = (int)B.slot[(2 * cp) * nt + k], rB = (int)B.slot[(2 * cp + 1) * nt + k];
                     if ((c & 1) && rA >= B.r0 && rA < B.r0 + rpc) continue;
-                    icm_pair<true, REPLAY, !REPLAY && (NARROW || !BLOCKTEAM)>(A, B, team, cp * D.nc + kk, rA, rB,
+                    icm_pair<true, REPLAY, !REPLAY && (NARROW || !BLOCKTEAM), !REPLAY && !BLOCKTEAM>(
+                                                                             A, B, team, cp * D.nc + kk, rA, rB,
                                                                              step, ls, X, 30, P);
                 }
             } else {

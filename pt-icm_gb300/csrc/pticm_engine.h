@@ -74,6 +74,8 @@ struct SmemPlan {
                                 // field from the neighbours' spins; ICM scratch and thresholds in device memory
     int32_t teams;              // ICM teams (warps, or one block-wide team)
     int32_t max_n_pad, max_kmax, max_R, max_nt;
+    int32_t icm_split;          // field_gather with several replicas: the block team's ICM scratch in shared
+                                // memory (at icm), its overlap list in device memory
 };
 
 // Trace of every random decision of the reference's sequential algorithm,

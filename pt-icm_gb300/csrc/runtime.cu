@@ -190,7 +190,9 @@ SmemPlan layout_plan(const PlanDims& d) {
     S.xpos = take(d.nt * 4);
     S.icm_team_bytes = icm_team_bytes((int32_t)d.max_n_pad);
     S.teams = d.teams;
-    S.icm = take((d.state_global || d.field_gather) ? 0 : d.icm_bytes);
+    S.icm_split = d.icm_split ? 1 : 0;
+    S.icm = take(d.icm_split ? (uint64_t)icm_team_bytes((int32_t)d.max_n_pad)
+                             : ((d.state_global || d.field_gather) ? 0 : d.icm_bytes));
     S.mag = take(d.rpc * 8);
     S.misc = take(64 + 8 * 32 + 4 * 64 + 64);
     S.total = (uint32_t)off;
@@ -202,11 +204,12 @@ SmemPlan layout_plan(const PlanDims& d) {
 }
 
 SmemPlan make_plan(const InstanceDesc& D, bool replay, int teams, int threads, bool stage_adj, bool state_global,
-                   bool field_gather) {
+                   bool field_gather, bool icm_split) {
     PlanDims d;
     d.replay = replay;
     d.state_global = state_global;
     d.field_gather = field_gather;
+    d.icm_split = field_gather && icm_split && teams == 1;
     d.add(D, stage_adj, teams);
     (void)threads;
     return layout_plan(d);
@@ -276,10 +279,42 @@ int choose_config(const HostProblem& P, const pticm_opts& o, bool replay, Instan
             return PTICM_ERR_UNSUPPORTED;
         }
         // first choice: the spins alone in shared memory, fields gathered
-        // at each visit (no field atomics), one replica per block
-        if (o.replicas_per_block == 0 && o.block_threads == 0) {
-            bool gathered = false;
-            for (int t : {1024, 512, 256, 128}) {
+        // at each visit (no field atomics).  Several replicas per block
+        // (each neighbour-list read serves all of them, and the cluster
+        // search's scratch fits in shared memory beside their spins) while
+        // the blocks still cover most SMs: on N=20000, R=512, four replicas
+        // in each of 128 blocks measured 11.1 G attempts/s against 8.7 G
+        // with one replica in each of 512 blocks.  Otherwise one replica per
+        // block, the largest block that keeps all R blocks resident.
+        auto gather_multi = [&](int rp) {
+            if (rp < 2 || R % rp != 0 || o.block_threads > (uint32_t)kNarrowThreads) return false;
+            const int t = o.block_threads ? (int)o.block_threads : kNarrowThreads;
+            InstanceDesc d1 = D;
+            d1.rpc = rp;
+            d1.group = R / rp;
+            for (bool split : {true, false}) {
+                const SmemPlan p1 = make_plan(d1, false, 1, t, false, false, true, split);
+                int per_sm = 0;
+                if (p1.total > kSmemLimit ||
+                    engine_max_blocks_per_sm(false, false, false, t, p1.total, &per_sm) != cudaSuccess ||
+                    (int64_t)per_sm * sms < R / rp)
+                    continue;
+                rpc = rp;
+                threads = t;
+                block_team = false;
+                teams = 1;
+                plan = p1;
+                return true;
+            }
+            return false;
+        };
+        auto gather_one = [&]() {
+            const int sizes[4] = {1024, 512, 256, 128};
+            const int asked[1] = {(int)o.block_threads};
+            const int* cand = o.block_threads ? asked : sizes;
+            const int ncand = o.block_threads ? 1 : 4;
+            for (int ci = 0; ci < ncand; ci++) {
+                const int t = cand[ci];
                 InstanceDesc d1 = D;
                 d1.rpc = 1;
                 d1.group = R;
@@ -293,13 +328,23 @@ int choose_config(const HostProblem& P, const pticm_opts& o, bool replay, Instan
                 block_team = true;
                 teams = 1;
                 plan = p1;
-                gathered = true;
-                break;
+                return true;
             }
-            if (gathered) {
-                cfg.field_gather = true;
-                break;
-            }
+            return false;
+        };
+        bool gathered = false;
+        if (o.replicas_per_block == 0) {
+            for (int rp : {4, 2})
+                if (!gathered && R / rp >= (3 * sms) / 4) gathered = gather_multi(rp);
+            if (!gathered) gathered = gather_one();
+        } else if (o.replicas_per_block == 1) {
+            gathered = gather_one();
+        } else {
+            gathered = gather_multi((int)o.replicas_per_block);
+        }
+        if (gathered) {
+            cfg.field_gather = true;
+            break;
         }
         global = true;
         // with the state in device memory a block needs little shared
@@ -458,7 +503,10 @@ int configure(pticm_ctx* c, bool replay) {
     c->plan = cfg.plan;
     finish_desc(c->desc, c->P, c->o, cfg);
     if (cfg.state_global || cfg.field_gather) {
-        c->icm_stride = (long long)icm_block_bytes(cfg.teams, c->desc.n_pad);
+        // (with the team scratch in shared memory only the overlap list and
+        // each list site's second overlap neighbour)
+        c->icm_stride = cfg.plan.icm_split ? (long long)(((uint64_t)c->desc.n_pad * 8 + 15) & ~15ull)
+                                           : (long long)icm_block_bytes(cfg.teams, c->desc.n_pad);
         const size_t want = (size_t)cfg.group * (size_t)c->icm_stride;
         if (c->d_icm_pool.n != want) CK(c->d_icm_pool.alloc(want));
     }

@@ -66,12 +66,12 @@ struct PlanDims {
     uint64_t n_stage = 0, nnz_stage = 0, ncolors = 0, n_h = 0, spin_sites = 0, nt_kst = 0, R = 0, rpc = 0, nt = 0,
              chains_m = 0, icm_bytes = 0, max_n_pad = 0, max_kmax = 0;
     int teams = 0;
-    bool stage = false, replay = false, state_global = false, field_gather = false;
+    bool stage = false, replay = false, state_global = false, field_gather = false, icm_split = false;
     void add(const InstanceDesc& D, bool stage_this, int teams_of_instance);
 };
 SmemPlan layout_plan(const PlanDims& d);
 SmemPlan make_plan(const InstanceDesc& D, bool replay, int teams, int threads, bool stage_adj,
-                   bool state_global = false, bool field_gather = false);
+                   bool state_global = false, bool field_gather = false, bool icm_split = false);
 constexpr uint32_t kSmemLimit = 232448 - 1024;   // 227 KB opt-in per block, less static smem
 
 int choose_config(const HostProblem& P, const pticm_opts& o, bool replay, InstanceDesc& D, LaunchConfig& cfg,

@@ -12,7 +12,9 @@ D\\C, so the pair must hold the oracle's two states exchanged exactly when
 Layouts: one replica per block (the block-team kernel, narrow 512-thread and
 wide 1024-thread variants, as the C1/C2 workloads run), several replicas per
 block with warp teams or a block-wide team, all replicas in one block, and
-the large-instance mode with spins in shared memory and fields gathered.
+the large-instance modes: spins in shared memory with fields gathered (one,
+two or four replicas per block) and the state in device memory (all in one
+block).
 """
 import os
 import zlib
@@ -57,6 +59,7 @@ LAYOUTS = {
     "block_team": dict(),                                   # one replica per block (C1/C2 layout)
     "block_team_1024": dict(block_threads=1024),            # wide block-team variant
     "two_per_block": dict(replicas_per_block=2),            # partners in other blocks, warp/block teams
+    "four_per_block": dict(replicas_per_block=4),           # (the large instance: fields gathered for 4)
     "one_block": dict(replicas_per_block=2 * NT),           # every replica in one block
 }
 
@@ -72,8 +75,6 @@ def test_icm_cluster_matches_oracle_bfs(graph, layout, algo, tmp_path_factory):
     prob = pticm.Problem.load(path)
     oprob = O.Problem.load(path, 0)
     n = prob.n
-    if graph == "random_20000_pm" and layout != "block_team":
-        pytest.skip("the large instance runs in its own layout only")
     rng = np.random.default_rng(zlib.crc32(f"{graph}/{layout}/{algo}".encode()))
     S = _pair_states(n, rng)
     # the oracle's result per pair and the seed drawn from its overlap
@@ -103,7 +104,10 @@ def test_icm_cluster_matches_oracle_bfs(graph, layout, algo, tmp_path_factory):
             raise
         lay = ctx.layout()
         if graph == "random_20000_pm":
-            assert lay.state_mode == 1, "the large instance gathers its fields"
+            # spins in shared memory with gathered fields while they fit;
+            # all 12 replicas in one block keep their state in device memory
+            want = 2 if lay.replicas_per_block > 4 else 1
+            assert lay.state_mode == want, (lay.replicas_per_block, lay.state_mode)
         if layout.startswith("block_team") and graph != "random_20000_pm":
             assert lay.block_team == 1 and lay.replicas_per_block == 1
         ctx.icm_pairs(seeds, exact=bool(exact))

@@ -155,7 +155,7 @@ def _gpu_block_runs(path, c, seeds, exchange, rpb):
 
 @pytest.mark.parametrize("exchange", [1, 0])
 @pytest.mark.parametrize("name,rpb", [("pmL20_c1", 1), ("pmL20_c1", 8), ("rnd200_w1", 1), ("rnd200_w1", 4),
-                                      ("rnd1000_pm", 1), ("rnd1000_pm", 4), ("c2", 1), ("c5_hot", 1)])
+                                      ("rnd1000_pm", 1), ("rnd1000_pm", 4), ("c2", 1), ("c5_hot", 1), ("c5_hot", 4)])
 def test_block_layouts_match_oracle_statistics(name, rpb, exchange, tmp_path):
     fx = _fixture(name)
     c = fx["config"]

@@ -159,6 +159,29 @@ def job_throughput(world, units_per_rank, max_ms):
     return world * units_per_rank / (max_ms / 1000.0)
 
 
+def phase_split(ctx, steps, pt_per_call):
+    """Where a PT step's time goes, after the timed region: the step time
+    with phases left out (sweep only; sweep and exchange; all), then the
+    in-kernel clock64 timers (pticm_set_profiling) over `steps` steps, us per
+    PT step (mean and max over blocks) and, for the ICM phases, per pair."""
+    out = {"masked_us_per_step": {}}
+    for mask, name in ((1, "sweep"), (3, "sweep+exchange"), (7, "all")):
+        ctx.run(pt_per_call, mask)
+        out["masked_us_per_step"][name] = ctx.stats()[0].last_run_ms * 1e3 / pt_per_call
+    ctx.set_profiling(True)
+    ctx.run(steps)
+    mean, mx = ctx.profile()
+    ctx.set_profiling(False)
+    pairs = max(mean["icm_pairs"], 1.0)
+    out["steps"] = steps
+    out["icm_pairs_per_block"] = mean["icm_pairs"] / steps
+    out["us_per_step"] = {k: [round(mean[k] * 1e3 / steps, 3), round(mx[k] * 1e3 / steps, 3)]
+                          for k in mean if k != "icm_pairs" and not k.startswith("x_")}
+    out["us_per_icm_pair"] = {k: round(mean[k] * 1e3 / pairs, 3) for k in mean
+                              if k.startswith(("icm", "uf")) and k != "icm_pairs"}
+    return out
+
+
 # ---------------------------------------------------------------- CPU legs
 def _cpu_sample(args):
     """One oracle solve (worker): CPU_WARM_PTS + warm PT steps untimed, then
@@ -278,6 +301,8 @@ def run_gpu(args, spec):
     total_ms = max_over_ranks(sum(dev_ms), dist, "cuda")
     value = job_throughput(world, attempts_per_step * args.steps, total_ms)
     mism = ctx.verify()
+    if args.phases and rank == 0:
+        print(json.dumps({"phase_split": phase_split(ctx, 2000, PT_PER_STEP)}), file=sys.stderr, flush=True)
 
     # end-to-end through the C ABI from host buffers, per step.  The input
     # states are the warmed-up replicas, each given to the replica that
@@ -542,6 +567,8 @@ def run_gpu_large(args):
             ctx.run(steps_per)
             dev_ms.append(ctx.stats()[0].last_run_ms)
     total_ms = sum(dev_ms)
+    if args.phases:
+        print(json.dumps({"phase_split": phase_split(ctx, 40, steps_per)}), file=sys.stderr, flush=True)
     sites = 4 * NTL * inst.n
     value = sites * steps_per * args.steps / (total_ms / 1000.0)
     mism = ctx.verify()
@@ -837,6 +864,8 @@ def main():
     ap.add_argument("--ttt-chunk", type=int, default=50)
     ap.add_argument("--ttt-max-steps", type=int, default=10000)
     ap.add_argument("--ttt-target-steps", type=int, default=10000)
+    ap.add_argument("--phases", action="store_true",
+                    help="c2/c1/large: after the timed region, print where a PT step's time goes (JSON, stderr)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args, SPECS.get(args.workload, SPECS["c2"]))

@@ -167,7 +167,6 @@ struct IcmScratch {
     uint8_t* d;
     uint32_t* vis;
     int* list;          // block team only: overlap sites first, the others from the end
-    int* link1;         // (device-memory list only) each list site's second overlap neighbour, or null
 };
 
 __device__ __forceinline__ IcmScratch icm_scratch(uint8_t* base, int n_pad) {
@@ -176,7 +175,6 @@ __device__ __forceinline__ IcmScratch icm_scratch(uint8_t* base, int n_pad) {
     X.d = base + (size_t)n_pad * 4;
     X.vis = reinterpret_cast<uint32_t*>(base + (size_t)n_pad * 5);
     X.list = reinterpret_cast<int*>(base + icm_team_bytes(n_pad));
-    X.link1 = nullptr;
     return X;
 }
 
@@ -528,11 +526,13 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                 // thread scans four of its sites side by side, so that
                 // their dependent loads overlap, then makes their unions)
                 const bool glink = GLINK && BLOCK && !__isShared(B.adj);
-                // (round 0 also finds each site's second overlap neighbour
-                // and keeps it, by list position, for round 1)
-                int* const link1 = glink ? X.link1 : nullptr;
+                // (a block team's round 0 also finds each site's second
+                // overlap neighbour and keeps it, by list position, in the
+                // free part of the list -- S is listed there only later --
+                // for round 1)
+                int* const link1 = (BLOCK && (LS || GLINK)) ? lst + sbase : nullptr;
                 for (int round = 0; round < 2; round++) {
-                    if (glink && round == 1 && link1 != nullptr) {
+                    if (round == 1 && link1 != nullptr) {
                         for (int t = team.tr; t < llen; t += 4 * team.ts) {
                             int u[4], tg[4];
 #pragma unroll
@@ -597,6 +597,31 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                                 if (round == 0 && link1 != nullptr) link1[t + k * team.ts] = t1[k];
                                 if (tg[k] >= 0) ok &= uf_unite(lab, u[k], tg[k]);
                             }
+                        }
+                    } else if (link1 != nullptr) {
+                        // round 0 of a block team: the first two overlap
+                        // neighbours, the list four entries at a time
+                        for (int t = team.tr; t < llen; t += team.ts) {
+                            const int u = lst[l0 + t];
+                            int k = 0, tgt = -1, t1 = -1;
+                            const int e1 = B.row[u + 1];
+                            for (int a = B.row[u]; a < e1 && k < 2; a += 4) {
+                                int v[4];
+                                bool on[4];
+#pragma unroll
+                                for (int j = 0; j < 4; j++) v[j] = a + j < e1 ? (int)(B.adj[a + j] >> 8) : u;
+#pragma unroll
+                                for (int j = 0; j < 4; j++) on[j] = a + j < e1 && d[v[j]];
+#pragma unroll
+                                for (int j = 0; j < 4; j++)
+                                    if (on[j] && k < 2) {
+                                        if (k == 0) tgt = v[j];
+                                        else t1 = v[j];
+                                        k++;
+                                    }
+                            }
+                            link1[t] = t1;
+                            if (tgt >= 0) ok &= uf_unite(lab, u, tgt);
                         }
                     } else
                     for_overlap([&](int u) {
@@ -1072,29 +1097,31 @@ __device__ void colored_sweep(const EngineArgs& A, const BlockCtx& B, unsigned l
                 int f[kGatherReps];
 #pragma unroll
                 for (int j = 0; j < kGatherReps; j++) f[j] = 0;
-                auto visit = [&](uint32_t e) {
+                // the neighbour list 16 bytes at a time, one load in flight
+                // (four spin loads per entry keep the thread busy)
+                auto scan = [&](auto&& visit) {
+                    int a = row[i];
+                    const int a1 = row[i + 1];
+                    if ((reinterpret_cast<uintptr_t>(adj) & 15u) == 0) {
+                        for (; a < a1 && (a & 3); a++) visit(adj[a]);
+#pragma unroll 1
+                        for (; a + 4 <= a1; a += 4) {
+                            const uint4 q = *reinterpret_cast<const uint4*>(adj + a);
+                            visit(q.x);
+                            visit(q.y);
+                            visit(q.z);
+                            visit(q.w);
+                        }
+                    }
+                    for (; a < a1; a++) visit(adj[a]);
+                };
+                scan([&](uint32_t e) {
                     const int w = (int)(int8_t)(e & 0xffu);
                     const int8_t* sn = B.spin + (e >> 8);
 #pragma unroll
                     for (int j = 0; j < kGatherReps; j++)
                         if (j < rpc) f[j] += w * sn[j * npad];
-                };
-                // the neighbour list 16 bytes at a time, one load in flight
-                // (four spin loads per entry keep the thread busy)
-                int a = row[i];
-                const int a1 = row[i + 1];
-                if ((reinterpret_cast<uintptr_t>(adj) & 15u) == 0) {
-                    for (; a < a1 && (a & 3); a++) visit(adj[a]);
-#pragma unroll 1
-                    for (; a + 4 <= a1; a += 4) {
-                        const uint4 q = *reinterpret_cast<const uint4*>(adj + a);
-                        visit(q.x);
-                        visit(q.y);
-                        visit(q.z);
-                        visit(q.w);
-                    }
-                }
-                for (; a < a1; a++) visit(adj[a]);
+                });
                 const int hi = D.has_h ? B.h[i] : 0;
 #pragma unroll
                 for (int j = 0; j < kGatherReps; j++) {
@@ -1731,10 +1758,8 @@ __global__ void __launch_bounds__((REPLAY || (BLOCKTEAM && !NARROW)) ? 1024 : kN
             if (BLOCKTEAM || D.teams == 1) {
                 const Team<true> team{tid, T, s_team_acc, s_team_bc};
                 IcmScratch X = icm_scratch(s_icm, npad);
-                if (!BLOCKTEAM && !REPLAY && S.icm_split) {
+                if (!BLOCKTEAM && !REPLAY && S.icm_split)
                     X.list = reinterpret_cast<int*>(A.icm_pool + (size_t)blockIdx.x * (size_t)A.icm_pool_stride);
-                    X.link1 = X.list + npad;
-                }
                 for (int j = 0; j < rpc; j++) {
                     const int sl = (int)B.rslot[j], c = sl / nt, k = sl - c * nt, kk = nt - 1 - k;
                     if (kk >= D.nc || c >= chains_even) continue;

@@ -503,9 +503,8 @@ int configure(pticm_ctx* c, bool replay) {
     c->plan = cfg.plan;
     finish_desc(c->desc, c->P, c->o, cfg);
     if (cfg.state_global || cfg.field_gather) {
-        // (with the team scratch in shared memory only the overlap list and
-        // each list site's second overlap neighbour)
-        c->icm_stride = cfg.plan.icm_split ? (long long)(((uint64_t)c->desc.n_pad * 8 + 15) & ~15ull)
+        // (with the team scratch in shared memory only the overlap list)
+        c->icm_stride = cfg.plan.icm_split ? (long long)(((uint64_t)c->desc.n_pad * 4 + 15) & ~15ull)
                                            : (long long)icm_block_bytes(cfg.teams, c->desc.n_pad);
         const size_t want = (size_t)cfg.group * (size_t)c->icm_stride;
         if (c->d_icm_pool.n != want) CK(c->d_icm_pool.alloc(want));

@@ -301,16 +301,19 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
         // (rows are n_pad bytes, a multiple of 16: every word is aligned)
         const int lane = threadIdx.x & 31;
         const int nq = (n + 3) >> 2;
+        // the next round's words are loaded before this round's are used
+        // (a partner's words come from its published copy in L2)
+        auto load_words = [&](int w, uint32_t& wa, uint32_t& wb) {
+            wa = locA ? reinterpret_cast<const uint32_t*>(sA)[w] : __ldcg(reinterpret_cast<const unsigned int*>(pubA) + w);
+            wb = locB ? reinterpret_cast<const uint32_t*>(sB)[w] : __ldcg(reinterpret_cast<const unsigned int*>(pubB) + w);
+        };
+        uint32_t na = 0, nb = 0;
+        if (team.tr < nq) load_words(team.tr, na, nb);
         for (int w0 = 0; w0 < nq; w0 += team.ts) {
             const int w = w0 + team.tr;
             const bool have = w < nq;
-            uint32_t wa = 0, wb = 0;
-            if (have) {
-                wa = locA ? reinterpret_cast<const uint32_t*>(sA)[w]
-                          : __ldcg(reinterpret_cast<const unsigned int*>(pubA) + w);
-                wb = locB ? reinterpret_cast<const uint32_t*>(sB)[w]
-                          : __ldcg(reinterpret_cast<const unsigned int*>(pubB) + w);
-            }
+            const uint32_t wa = na, wb = nb;
+            if (w + team.ts < nq) load_words(w + team.ts, na, nb);
             uint32_t dw = 0;
             int fm = 0, bm = 0;
             if (have) {
@@ -585,13 +588,20 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
 #pragma unroll
                             for (int k = 0; k < 4; k++) {
                                 if (u[k] < 0) continue;
-                                // rarely: the targets lie past the first four entries
-                                for (int aa = a[k] + 4; aa < e[k] && k4[k] < want; aa++) {
-                                    const int w = (int)(B.adj[aa] >> 8);
-                                    if (d[w]) {
-                                        if (k4[k] == round) tg[k] = w;
-                                        else if (k4[k] == round + 1) t1[k] = w;
-                                        k4[k]++;
+                                // the targets past the first four entries: four
+                                // independent loads at a time
+                                for (int aa = a[k] + 4; aa < e[k] && k4[k] < want; aa += 4) {
+                                    uint32_t w4[4];
+#pragma unroll
+                                    for (int j = 0; j < 4; j++) w4[j] = aa + j < e[k] ? B.adj[aa + j] : 0xFFFFFFFFu;
+#pragma unroll
+                                    for (int j = 0; j < 4; j++) {
+                                        const bool on = w4[j] != 0xFFFFFFFFu && d[w4[j] >> 8];
+                                        if (on && k4[k] < want) {
+                                            if (k4[k] == round) tg[k] = (int)(w4[j] >> 8);
+                                            else if (k4[k] == round + 1) t1[k] = (int)(w4[j] >> 8);
+                                            k4[k]++;
+                                        }
                                     }
                                 }
                                 if (round == 0 && link1 != nullptr) link1[t + k * team.ts] = t1[k];

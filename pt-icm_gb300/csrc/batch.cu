@@ -51,6 +51,7 @@ constexpr double kLaunchTargetUs = 500000.0;   // aim: one launch ~0.5 s, a quar
 
 struct pticm_batch {
     std::vector<HostProblem> P;
+    long long ebound = -1;      // largest energy_bound over the instances, once
     pticm_opts o{};
     int count = 0, nt = 0, C = 0, R = 0, threads = 1024;
     std::vector<InstanceDesc> desc;
@@ -301,6 +302,11 @@ EngineArgs batch_args(pticm_batch* b) {
     A.attempts = b->d_att.p;
     A.successes = b->d_succ.p;
     A.bar = b->d_bar.p;
+    if (b->ebound < 0) {
+        b->ebound = 0;
+        for (const HostProblem& P : b->P) b->ebound = std::max(b->ebound, energy_bound(P));
+    }
+    A.flag_barrier = b->ebound < (1ll << 31) ? 1 : 0;   // every energy fits the word's 32 bits
     A.abort_flag = b->d_abort.p;
     A.status = b->d_status.p;
     A.sweeps = (int)b->o.sweeps;

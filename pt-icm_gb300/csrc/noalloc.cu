@@ -266,6 +266,7 @@ extern "C" int pticm_run_noalloc(const pticm_problem* p, const pticm_opts* o, co
     A.attempts = reinterpret_cast<unsigned long long*>(base + o_att);
     A.successes = reinterpret_cast<unsigned long long*>(base + o_succ);
     A.bar = reinterpret_cast<unsigned int*>(base + o_bar);
+    A.flag_barrier = energy_bound(P) < (1ll << 31) ? 1 : 0;   // every energy fits the word's 32 bits
     A.abort_flag = reinterpret_cast<int*>(base + o_abort);
     A.status = reinterpret_cast<DevStatus*>(base + o_status);
     A.sweeps = (int)o->sweeps;

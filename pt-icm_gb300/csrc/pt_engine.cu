@@ -21,6 +21,8 @@
 // the host in FP64.  The replay variant visits sites in the reference's
 // sequential order and consumes a recorded uniform stream with FP64
 // exp(-beta*dE) tables, reproducing the reference bit for bit.
+#include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 
@@ -1709,7 +1711,54 @@ __global__ void __launch_bounds__((REPLAY || (BLOCKTEAM && !NARROW)) ? 1024 : kN
                 for (int j = tid; j < rpc; j += T)
                     A.mag_pub[parity * A.energy_pub_half + D.rep_off + B.r0 + j] = s_mag[j];
         }
-        if (D.group > 1) {
+        if (D.group > 1 && A.flag_barrier) {
+            // publish this block's spins (for ICM partners), then each of its
+            // replicas' energy tagged with this step in one 64-bit word,
+            // stored with release; wait for every other replica's word of
+            // this step, acquiring its block's spins with it.  No counter
+            // to arrive at and no second hop: a block goes on as soon as the
+            // last word it needs lands, holding the energies it read.
+            if (icm_on) {
+                const long long base = parity * A.spins_pub_half + D.spin_off + (long long)B.r0 * npad;
+                for (int idx = tid; idx < rpc * npad; idx += T) A.spins_pub[base + idx] = B.spin[idx];
+            }
+            __syncthreads();
+            unsigned long long* const ew =
+                reinterpret_cast<unsigned long long*>(A.energy_pub + parity * A.energy_pub_half + D.rep_off);
+            const uint32_t tag = A.pub_base + (uint32_t)ls;
+            for (int j = tid; j < rpc; j += T) st_release_gpu_u64(ew + B.r0 + j, pub_word(tag, B.E[B.r0 + j]));
+            const unsigned long long limit = A.wait_limit_ns ? A.wait_limit_ns : kWaitLimitNs;
+            int ok = 1;
+            for (int r = tid; r < R && ok; r += T) {
+                if (r >= B.r0 && r < B.r0 + rpc) continue;
+                const unsigned long long t0 = globaltimer_ns();
+                unsigned int spins = 0;
+                unsigned long long w;
+                while ((uint32_t)((w = ld_relaxed_gpu_u64(ew + r)) >> 32) != tag) {
+                    if (*abortf) { ok = 0; break; }
+                    if ((++spins & 63u) == 0 && globaltimer_ns() - t0 > limit) {
+                        dev_fail(A.status, A.abort_flag, DEV_BARRIER_TIMEOUT, 1, blockIdx.x, tag);
+                        ok = 0;
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+                if (ok) B.E[r] = (long long)(int32_t)(uint32_t)w;
+            }
+            if (A.bar_phantom && tid == 0 && ok) {
+                // test hook: one more member whose word never comes
+                const unsigned long long t0 = globaltimer_ns();
+                while (ok) {
+                    if (*abortf) ok = 0;
+                    else if (globaltimer_ns() - t0 > limit) {
+                        dev_fail(A.status, A.abort_flag, DEV_BARRIER_TIMEOUT, 1, blockIdx.x, tag);
+                        ok = 0;
+                    } else __nanosleep(256);
+                }
+            }
+            fence_acq_rel_gpu();   // (the words were read relaxed: acquire what they publish)
+            if (!__syncthreads_and(ok)) break;
+        } else if (D.group > 1) {
             // publish this block's energies (and spins, for ICM partners)
             for (int j = tid; j < rpc; j += T) A.energy_pub[parity * A.energy_pub_half + D.rep_off + B.r0 + j] = B.E[B.r0 + j];
             if (icm_on) {
@@ -1989,11 +2038,20 @@ static void* engine_fn(bool replay, bool block_team, bool narrow) {
     return (void*)pt_engine_kernel<false, false, false>;
 }
 
-cudaError_t launch_engine(const EngineArgs& A, int threads, bool replay, bool block_team, bool narrow,
+// Tags of published energy words: one per PT step of every launch in the
+// process, never 0 (a zeroed word) and never repeated within 2^32 steps.
+static std::atomic<uint32_t> g_pub_tag{1u};
+
+cudaError_t launch_engine(const EngineArgs& A0, int threads, bool replay, bool block_team, bool narrow,
                           bool cooperative, cudaStream_t stream) {
     void* fn = engine_fn(replay, block_team, narrow);
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)A.sm.total);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)A0.sm.total);
     if (e != cudaSuccess) return e;
+    EngineArgs A = A0;
+    const uint32_t span = (uint32_t)std::max(A.nsteps, 1) + 1u;
+    uint32_t base = g_pub_tag.fetch_add(span);
+    if (base == 0u || base + span < base) base = g_pub_tag.fetch_add(span);   // (past the wrap: 0 stays unused)
+    A.pub_base = base;
     void* args[] = {(void*)&A};
     if (cooperative)
         return cudaLaunchCooperativeKernel(fn, dim3(A.n_blocks), dim3(threads), args, A.sm.total, stream);

@@ -190,6 +190,29 @@ __device__ __forceinline__ void red_add_release_gpu(unsigned int* p, unsigned in
     asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(x) : "memory");
 }
 
+__device__ __forceinline__ unsigned long long ld_relaxed_gpu_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_gpu_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ void fence_acq_rel_gpu() {
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+}
+
+// A replica's published energy word: the publishing step's tag in the high
+// half, the energy (it fits 32 bits: the launch checks the problem's energy
+// range) in the low half.  Tags come from a counter that never repeats and
+// never gives 0, so neither a zeroed word nor one left by an earlier step or
+// launch matches the tag being waited for.
+__device__ __forceinline__ unsigned long long pub_word(uint32_t tag, long long E) {
+    return ((unsigned long long)tag << 32) | (unsigned long long)(uint32_t)(int32_t)E;
+}
+
 // A counting barrier over `nblocks` co-resident blocks (guaranteed by a
 // cooperative launch).  Arrivals are counted in bar[0] with an acquire-
 // release add (it publishes the block's writes, ordered before it by the

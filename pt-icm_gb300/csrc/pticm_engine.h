@@ -164,6 +164,12 @@ struct EngineArgs {
     // barrier's wait run out)
     int32_t bar_phantom;
     unsigned long long wait_limit_ns;
+    // The per-step exchange of a group's energies: 1 = tagged energy words
+    // (energy_pub holds tag << 32 | energy; every energy of the problem fits
+    // 32 bits), 0 = the counting group barrier, then plain energy loads.
+    // pub_base + (step within the launch) is the tag; launch_engine sets it.
+    int32_t flag_barrier;
+    uint32_t pub_base;
 };
 
 enum EngineFlags : int32_t {

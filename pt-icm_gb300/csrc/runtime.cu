@@ -106,6 +106,7 @@ struct pticm_ctx {
     DArr<uint8_t> d_states_in;  // caller states in the original site order (pticm_set_states)
     DArr<uint8_t> d_icm_pool;   // ICM scratch when the replicas live in device memory
     long long icm_stride = 0;
+    long long ebound = -1;      // energy_bound(P), once
     DArr<long long> d_icm_force;   // per-pair seeds of pticm_icm_pairs
     // bounded waits: limit (0 = kWaitLimitNs) and the barrier test hook
     unsigned long long wait_limit_ns = 0;
@@ -570,6 +571,8 @@ EngineArgs make_args(pticm_ctx* c) {
     A.icm_pool_stride = c->icm_stride;
     A.wait_limit_ns = c->wait_limit_ns;
     A.bar_phantom = c->bar_phantom;
+    if (c->ebound < 0) c->ebound = energy_bound(c->P);
+    A.flag_barrier = c->ebound < (1ll << 31) ? 1 : 0;   // every energy fits the word's 32 bits
     return A;
 }
 

@@ -503,7 +503,7 @@ int pticm_batch_create(const pticm_problem* const* problems, uint32_t count, con
     BCK(b->d_best_state.alloc(spin_total));
     BCK(b->d_pub.alloc(2 * spin_total));
     BCK(b->d_E.alloc(rep_total));
-    BCK(b->d_Epub.alloc(2 * rep_total));
+    BCK(b->d_Epub.alloc(2 * rep_total * kPubStride));
     BCK(b->d_bestE.alloc(rep_total));
     BCK(b->d_flips.alloc(rep_total));
     BCK(b->d_bestSweep.alloc(rep_total));

@@ -167,7 +167,7 @@ extern "C" int pticm_run_noalloc(const pticm_problem* p, const pticm_opts* o, co
     const size_t o_h = cv.take((n + 4) * 4), o_perm = cv.take((n + 4) * 4), o_beta = cv.take((size_t)nt * 8);
     const size_t o_thr = cv.take(thr.size() * 4 + 16);
     const size_t o_spins = cv.take(RR * npad), o_fields = cv.take(RR * npad * 4), o_E = cv.take(RR * 8);
-    const size_t o_pub = cv.take(2 * RR * npad), o_Epub = cv.take(2 * RR * 8);
+    const size_t o_pub = cv.take(2 * RR * npad), o_Epub = cv.take(2 * RR * 8 * kPubStride);
     const size_t o_flips = cv.take(RR * 8), o_bestE = cv.take(RR * 8), o_bestS = cv.take(RR * 8);
     const size_t o_bstate = cv.take(RR * npad), o_slot = cv.take(RR * 4), o_order = cv.take((size_t)nt * 4);
     const size_t o_att = cv.take(RR * 8), o_succ = cv.take(RR * 8);

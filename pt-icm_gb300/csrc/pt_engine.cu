@@ -1016,26 +1016,34 @@ __device__ void colored_sweep(const EngineArgs& A, const BlockCtx& B, unsigned l
     unsigned acc_fl = 0;
     // several replicas in the block, fields gathered
     const bool gm = !ONE && B.field == nullptr && rpc <= kGatherReps;
-    for (int c = 0; c < D.ncolors; c++) {
+    // the one-replica sweep's pointers and flags, read once from the
+    // block's shared context (the compiler may not keep them across the
+    // stores of a colour class)
+    int8_t* const sp1 = B.spin;
+    int32_t* const fd1 = B.field;
+    const int32_t* const h1 = D.has_h ? B.h : nullptr;
+    const uint32_t* const thr1 = ONE ? s_thr + B.tb[0] : s_thr;
+    const int ncolors = D.ncolors;
+    for (int c = 0; c < ncolors; c++) {
         const int c0 = s_col[c];
         const int Sc = s_col[c + 1] - c0;
-        if (ONE && COOP && B.field) {
+        if (ONE && COOP && fd1 != nullptr) {
             // each thread decides its own site (the same site and random
             // draws as one site per thread).  A warp with few accepted sites
             // (the cold replicas) pushes their field changes one site at a
             // time with a lane per neighbour, so that no lane walks a long
             // neighbour list alone; a warp with many (the hot replicas)
             // lets every lane push its own site's changes, side by side
-            int8_t* sp = B.spin;
-            int32_t* fd = B.field;
-            const uint32_t* thr_row = s_thr + B.tb[0];
+            int8_t* const sp = sp1;
+            int32_t* const fd = fd1;
+            const uint32_t* const thr_row = thr1;
             for (int base = c0 + (tid & ~31); base < c0 + Sc; base += T) {
                 const int i = base + lane;
                 bool acc = false;
                 int s = 0, e0 = 0, e1 = 0;
                 if (i < c0 + Sc) {
                     s = sp[i];
-                    const int f = fd[i] + (D.has_h ? B.h[i] : 0);
+                    const int f = fd[i] + (h1 != nullptr ? h1[i] : 0);
                     const int de = -2 * s * f;
                     acc = de <= 0;
                     if (!acc) {
@@ -1723,18 +1731,21 @@ __global__ void __launch_bounds__((REPLAY || (BLOCKTEAM && !NARROW)) ? 1024 : kN
                 for (int idx = tid; idx < rpc * npad; idx += T) A.spins_pub[base + idx] = B.spin[idx];
             }
             __syncthreads();
-            unsigned long long* const ew =
-                reinterpret_cast<unsigned long long*>(A.energy_pub + parity * A.energy_pub_half + D.rep_off);
+            unsigned long long* const ew = reinterpret_cast<unsigned long long*>(A.energy_pub) +
+                                           (parity * A.energy_pub_half + D.rep_off) * kPubStride;
             const uint32_t tag = A.pub_base + (uint32_t)ls;
-            for (int j = tid; j < rpc; j += T) st_release_gpu_u64(ew + B.r0 + j, pub_word(tag, B.E[B.r0 + j]));
+            for (int j = tid; j < rpc; j += T)
+                st_release_gpu_u64(ew + (B.r0 + j) * kPubStride, pub_word(tag, B.E[B.r0 + j]));
             const unsigned long long limit = A.wait_limit_ns ? A.wait_limit_ns : kWaitLimitNs;
             int ok = 1;
+            bool polled = false;
             for (int r = tid; r < R && ok; r += T) {
                 if (r >= B.r0 && r < B.r0 + rpc) continue;
+                polled = true;
                 const unsigned long long t0 = globaltimer_ns();
                 unsigned int spins = 0;
                 unsigned long long w;
-                while ((uint32_t)((w = ld_relaxed_gpu_u64(ew + r)) >> 32) != tag) {
+                while ((uint32_t)((w = ld_relaxed_gpu_u64(ew + r * kPubStride)) >> 32) != tag) {
                     if (*abortf) { ok = 0; break; }
                     if ((++spins & 63u) == 0 && globaltimer_ns() - t0 > limit) {
                         dev_fail(A.status, A.abort_flag, DEV_BARRIER_TIMEOUT, 1, blockIdx.x, tag);
@@ -1756,7 +1767,9 @@ __global__ void __launch_bounds__((REPLAY || (BLOCKTEAM && !NARROW)) ? 1024 : kN
                     } else __nanosleep(256);
                 }
             }
-            fence_acq_rel_gpu();   // (the words were read relaxed: acquire what they publish)
+            // the words were read relaxed: each thread that read one acquires
+            // what its release published (the block's barrier passes it on)
+            if (polled) fence_acq_rel_gpu();
             if (!__syncthreads_and(ok)) break;
         } else if (D.group > 1) {
             // publish this block's energies (and spins, for ICM partners)

@@ -196,12 +196,12 @@ __device__ __forceinline__ unsigned long long ld_relaxed_gpu_u64(const unsigned 
     return v;
 }
 
-__device__ __forceinline__ void st_release_gpu_u64(unsigned long long* p, unsigned long long v) {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-
 __device__ __forceinline__ void fence_acq_rel_gpu() {
     asm volatile("fence.acq_rel.gpu;" ::: "memory");
+}
+
+__device__ __forceinline__ void st_release_gpu_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
 // A replica's published energy word: the publishing step's tag in the high

@@ -114,7 +114,7 @@ struct EngineArgs {
     long long* energy;
     int8_t* spins_pub;            // 2 halves, parity of the PT step
     long long spins_pub_half;     // elements per half
-    long long* energy_pub;        // 2 * total replicas
+    long long* energy_pub;        // 2 * total replicas (x kPubStride words with flag_barrier)
     long long energy_pub_half;
     unsigned long long* flips;
     long long* best_E;
@@ -188,6 +188,10 @@ enum EngineFlags : int32_t {
 // Threads of a block of several replicas, or of a block team launched with
 // the narrow bound (120 registers a thread).
 constexpr int kNarrowThreads = 512;
+// Published energy words (flag_barrier) sit one per 128-byte line, so that
+// the blocks polling a group's words do not all queue on a few lines:
+// energy_pub holds 2 * replicas * kPubStride words.
+constexpr int kPubStride = 16;
 
 inline constexpr uint32_t icm_team_bytes(int32_t n_pad) {
     return (uint32_t)((((uint64_t)n_pad * 5 + 4 * (((uint64_t)n_pad + 31) / 32)) + 15) & ~15ull);

@@ -985,7 +985,7 @@ int pticm_create(const pticm_problem* p, const pticm_opts* o, pticm_ctx** out) {
     CK(c->d_best_state.alloc(spins));
     CK(c->d_pub.alloc(2 * spins));
     CK(c->d_E.alloc(c->R));
-    CK(c->d_Epub.alloc(2 * c->R));
+    CK(c->d_Epub.alloc(2 * c->R * kPubStride));
     CK(c->d_bestE.alloc(c->R));
     CK(c->d_flips.alloc(c->R));
     CK(c->d_bestSweep.alloc(c->R));

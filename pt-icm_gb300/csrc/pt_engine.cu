@@ -226,6 +226,12 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                          int where_err, Prof& P) {
     const InstanceDesc& D = B.D;
     const int n = D.n, npad = D.n_pad;
+    // the block context lives in shared memory: its pointers and flags are
+    // read once here, not at every use inside the passes' loops
+    const int32_t* const brow = B.row;
+    const uint32_t* const badj = B.adj;
+    const int32_t* const bh = D.has_h ? B.h : nullptr;
+    const bool has_h = bh != nullptr;
     const bool locA = rA >= B.r0 && rA < B.r0 + D.rpc;
     const bool locB = rB >= B.r0 && rB < B.r0 + D.rpc;
     const int parity = (int)(step & 1ull);
@@ -273,7 +279,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
             if (di) kd = min(kd, key);
             else ke = min(ke, key);
         }
-        if (D.has_h && locA) hs += (long long)B.h[i] * a;
+        if (has_h && locA) hs += (long long)bh[i] * a;
     };
     // a block team lists the overlap sites (from the front) and the others
     // (from the back), so that its later passes visit overlap sites only;
@@ -334,7 +340,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                         (unsigned)i;
                     if (di) kd = min(kd, key);
                     else ke = min(ke, key);
-                    if (D.has_h && locA) hs += (long long)B.h[i] * a;
+                    if (has_h && locA) hs += (long long)bh[i] * a;
                 }
                 reinterpret_cast<uint32_t*>(d)[w] = dw;
                 if (algo == ENGINE_ICM_UNION_FIND)   // union-find parents
@@ -478,13 +484,13 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                     const int idx = base + team.tr;
                     const bool have = idx < hi;
                     const int u = have ? X.queue[idx] : 0;
-                    const int e0 = have ? B.row[u] : 0;
-                    const int deg = have ? B.row[u + 1] - e0 : 0;
+                    const int e0 = have ? brow[u] : 0;
+                    const int deg = have ? brow[u + 1] - e0 : 0;
                     for (int k = 0; __any_sync(0xffffffffu, k < deg); k++) {
                         bool found = false;
                         int v = 0;
                         if (k < deg) {
-                            v = (int)(B.adj[e0 + k] >> 8);
+                            v = (int)(badj[e0 + k] >> 8);
                             if (((volatile uint8_t*)d)[v] == 1) {
                                 const uint32_t bit = 1u << (v & 31);
                                 found = !(atomicOr(X.vis + (v >> 5), bit) & bit);
@@ -530,7 +536,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                 // (GLINK: with the neighbour lists in device memory, a
                 // thread scans four of its sites side by side, so that
                 // their dependent loads overlap, then makes their unions)
-                const bool glink = GLINK && BLOCK && !__isShared(B.adj);
+                const bool glink = GLINK && BLOCK && !__isShared(badj);
                 // (a block team's round 0 also finds each site's second
                 // overlap neighbour and keeps it, by list position, in the
                 // free part of the list -- S is listed there only later --
@@ -560,14 +566,14 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                             }
 #pragma unroll
                             for (int k = 0; k < 4; k++) {
-                                a[k] = u[k] >= 0 ? B.row[u[k]] : 0;
-                                e[k] = u[k] >= 0 ? B.row[u[k] + 1] : 0;
+                                a[k] = u[k] >= 0 ? brow[u[k]] : 0;
+                                e[k] = u[k] >= 0 ? brow[u[k] + 1] : 0;
                             }
                             uint32_t v[4][4];
 #pragma unroll
                             for (int k = 0; k < 4; k++)
 #pragma unroll
-                                for (int j = 0; j < 4; j++) v[k][j] = a[k] + j < e[k] ? B.adj[a[k] + j] : 0xFFFFFFFFu;
+                                for (int j = 0; j < 4; j++) v[k][j] = a[k] + j < e[k] ? badj[a[k] + j] : 0xFFFFFFFFu;
                             // the round-th overlap neighbour (tg) and, in
                             // round 0 with a place to keep it, the next (t1)
                             const int want = (round == 0 && link1 != nullptr) ? 2 : round + 1;
@@ -595,7 +601,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                                 for (int aa = a[k] + 4; aa < e[k] && k4[k] < want; aa += 4) {
                                     uint32_t w4[4];
 #pragma unroll
-                                    for (int j = 0; j < 4; j++) w4[j] = aa + j < e[k] ? B.adj[aa + j] : 0xFFFFFFFFu;
+                                    for (int j = 0; j < 4; j++) w4[j] = aa + j < e[k] ? badj[aa + j] : 0xFFFFFFFFu;
 #pragma unroll
                                     for (int j = 0; j < 4; j++) {
                                         const bool on = w4[j] != 0xFFFFFFFFu && d[w4[j] >> 8];
@@ -616,12 +622,12 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                         for (int t = team.tr; t < llen; t += team.ts) {
                             const int u = lst[l0 + t];
                             int k = 0, tgt = -1, t1 = -1;
-                            const int e1 = B.row[u + 1];
-                            for (int a = B.row[u]; a < e1 && k < 2; a += 4) {
+                            const int e1 = brow[u + 1];
+                            for (int a = brow[u]; a < e1 && k < 2; a += 4) {
                                 int v[4];
                                 bool on[4];
 #pragma unroll
-                                for (int j = 0; j < 4; j++) v[j] = a + j < e1 ? (int)(B.adj[a + j] >> 8) : u;
+                                for (int j = 0; j < 4; j++) v[j] = a + j < e1 ? (int)(badj[a + j] >> 8) : u;
 #pragma unroll
                                 for (int j = 0; j < 4; j++) on[j] = a + j < e1 && d[v[j]];
 #pragma unroll
@@ -640,12 +646,12 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                         // the neighbour list four entries at a time: four
                         // independent loads, then four flag loads
                         int k = 0, tgt = -1;
-                        const int e1 = B.row[u + 1];
-                        for (int a = B.row[u]; a < e1 && tgt < 0; a += 4) {
+                        const int e1 = brow[u + 1];
+                        for (int a = brow[u]; a < e1 && tgt < 0; a += 4) {
                             int v[4];
                             bool on[4];
 #pragma unroll
-                            for (int j = 0; j < 4; j++) v[j] = a + j < e1 ? (int)(B.adj[a + j] >> 8) : u;
+                            for (int j = 0; j < 4; j++) v[j] = a + j < e1 ? (int)(badj[a + j] >> 8) : u;
 #pragma unroll
                             for (int j = 0; j < 4; j++) on[j] = a + j < e1 && d[v[j]];
 #pragma unroll
@@ -734,10 +740,10 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                         if (pos < llen) lst[sbase + pos] = u;
                         return;
                     }
-                    const int e1 = B.row[u + 1];
+                    const int e1 = brow[u + 1];
 #pragma unroll 4
-                    for (int a = B.row[u]; a < e1; a++) {
-                        const int v = (int)(B.adj[a] >> 8);
+                    for (int a = brow[u]; a < e1; a++) {
+                        const int v = (int)(badj[a] >> 8);
                         if (d[v]) ok &= uf_unite(lab, u, v);
                     }
                 });
@@ -754,9 +760,9 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                     const int a0 = by_warp ? team.tr & 31 : 0, da = by_warp ? 32 : 1;
                     for (int t = t0; t < ns0; t += dt) {
                         const int u = lst[sbase + t];
-                        const int e1 = B.row[u + 1];
-                        for (int a = B.row[u] + a0; a < e1; a += da) {
-                            const int v = (int)(B.adj[a] >> 8);
+                        const int e1 = brow[u + 1];
+                        for (int a = brow[u] + a0; a < e1; a += da) {
+                            const int v = (int)(badj[a] >> 8);
                             if (d[v]) ok &= uf_unite(lab, u, v);
                         }
                     }
@@ -798,10 +804,10 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                         if (!d[u]) continue;
                         const int lu = vl[u];
                         int best = lu;
-                        const int e1 = B.row[u + 1];
+                        const int e1 = brow[u + 1];
 #pragma unroll 4
-                        for (int a = B.row[u]; a < e1; a++) {
-                            const int v = (int)(B.adj[a] >> 8);
+                        for (int a = brow[u]; a < e1; a++) {
+                            const int v = (int)(badj[a] >> 8);
                             const int lv = vl[v];
                             if (d[v]) best = min(best, lv);
                         }
@@ -874,7 +880,7 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
         // (by_warp: the lanes of a warp share the site, read its spins
         // before lane 0 flips them and take every 32nd edge)
         auto flip_push = [&](int u, bool by_warp) {
-            const int hu = D.has_h ? B.h[u] : 0;
+            const int hu = has_h ? bh[u] : 0;
             const int lane = by_warp ? (threadIdx.x & 31) : 0;
             int sa = 0, sb = 0;   // spins before the flip
             if (locA) sa = sA[u];
@@ -884,10 +890,10 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
                 if (locA) { sA[u] = (int8_t)-sa; dEa -= 2 * sa * hu; }
                 if (locB) { sB[u] = (int8_t)-sb; dEb -= 2 * sb * hu; }
             }
-            const int e1 = B.row[u + 1], da = by_warp ? 32 : 1;
+            const int e1 = brow[u + 1], da = by_warp ? 32 : 1;
 #pragma unroll 4
-            for (int a = B.row[u] + lane; a < e1; a += da) {
-                const uint32_t e = B.adj[a];
+            for (int a = brow[u] + lane; a < e1; a += da) {
+                const uint32_t e = badj[a];
                 const int v = (int)(e >> 8);
                 const int J = (int)(int8_t)(e & 0xffu);
                 if (fA) atomicAdd(fA + v, J * (-2 * sa));
@@ -921,16 +927,16 @@ __device__ int icm_pair(const EngineArgs& A, const BlockCtx& B, const Team<BLOCK
             long long eA = 0, eB = 0;
             for (int i = team.tr; i < n; i += team.ts) {
                 int fa = 0, fb = 0;
-                const int e1 = B.row[i + 1];
+                const int e1 = brow[i + 1];
 #pragma unroll 4
-                for (int a = B.row[i]; a < e1; a++) {
-                    const uint32_t e = B.adj[a];
+                for (int a = brow[i]; a < e1; a++) {
+                    const uint32_t e = badj[a];
                     const int v = (int)(e >> 8);
                     const int J = (int)(int8_t)(e & 0xffu);
                     if (locA) fa += J * sA[v];
                     if (locB) fb += J * sB[v];
                 }
-                const int h2 = D.has_h ? 2 * B.h[i] : 0;
+                const int h2 = has_h ? 2 * bh[i] : 0;
                 if (locA) { if (fA) fA[i] = fa; eA += (long long)sA[i] * (h2 + fa); }
                 if (locB) { if (fB) fB[i] = fb; eB += (long long)sB[i] * (h2 + fb); }
             }

@@ -199,7 +199,8 @@ PTICM_API int pticm_get_exchange_order(pticm_ctx* c, uint32_t* order);
  * of a PT step) or on bulk copies gives up after limit_ns (0: the default,
  * 2 s), records where, and the call returns PTICM_ERR_DEVICE; the context
  * stays usable.  phantom_arrivals = 1 is a test hook: every group barrier
- * then waits for one block more than it has, so each of its waits runs out
+ * then waits for one member more than it has (a block, or a replica's
+ * energy word, that never arrives), so each of its waits runs out
  * (the reference has no failure detection: src/initialization.cc:120-126 and
  * src/mpi_utils.cc:223-225 assert or exit). */
 PTICM_API int pticm_set_wait_limit(pticm_ctx* c, uint64_t limit_ns, uint32_t phantom_arrivals);

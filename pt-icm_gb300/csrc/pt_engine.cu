@@ -1457,23 +1457,43 @@ __device__ void exchange_even_odd(const EngineArgs& A, const BlockCtx& B, unsign
     const InstanceDesc& D = B.D;
     const int tid = threadIdx.x, T = blockDim.x;
     const int nt = D.nt, C = D.chains, m = nt - 1;
+    const uint32_t inst = (uint32_t)D.inst_id;
+    uint32_t* const slot = B.slot;
+    const long long* const E = B.E;
     const uint2 key = stream_key(A.seed, STREAM_EXCHANGE);
+    auto log_u = [&](int k, int par) {
+        const uint4 r = philox4x32_10(make_uint4((uint32_t)(k | (par << 30)), inst, (uint32_t)step, (uint32_t)(step >> 32)), key);
+        return __logf(u01_open0(r.x));
+    };
+    auto pair_of = [&](int t, int par, int per_chain, int& kb) {
+        const int c = t / per_chain;
+        kb = par + 2 * (t - c * per_chain);
+        return c * nt + kb;
+    };
+    // when each pass has at most one pair per thread, both passes' draws
+    // are made first, side by side (they do not depend on the energies)
+    const int per0 = (m + 1) / 2, per1 = m / 2;
+    const bool one = C * per0 <= T;
+    float lu0 = 0.f, lu1 = 0.f;
+    if (one) {
+        int kb;
+        if (tid < C * per0) lu0 = log_u(pair_of(tid, 0, per0, kb), 0);
+        if (tid < C * per1) lu1 = log_u(pair_of(tid, 1, per1, kb), 1);
+    }
     for (int par = 0; par < 2; par++) {
-        const int per_chain = (m - par + 1) / 2;   // pairs kb = par, par+2, ...
+        const int per_chain = par ? per1 : per0;   // pairs kb = par, par+2, ...
         const int total = C * per_chain;
         for (int t = tid; t < total; t += T) {
-            const int c = t / per_chain;
-            const int kb = par + 2 * (t - c * per_chain);
-            const int k = c * nt + kb;
-            const uint4 r = philox4x32_10(make_uint4((uint32_t)(k | (par << 30)), (uint32_t)D.inst_id,
-                                                     (uint32_t)step, (uint32_t)(step >> 32)), key);
-            const uint32_t r1 = B.slot[k], r2 = B.slot[k + 1];
-            const double x = s_dbeta[kb] * (double)(B.E[r1] - B.E[r2]);
+            int kb;
+            const int k = pair_of(t, par, per_chain, kb);
+            const float lu = one ? (par ? lu1 : lu0) : log_u(k, par);
+            const uint32_t r1 = slot[k], r2 = slot[k + 1];
+            const double x = s_dbeta[kb] * (double)(E[r1] - E[r2]);
             s_att[k]++;
-            if (x > 0.0 || (double)__logf(u01_open0(r.x)) < x) {
+            if (x > 0.0 || (double)lu < x) {
                 s_succ[k]++;
-                B.slot[k] = r2;
-                B.slot[k + 1] = r1;
+                slot[k] = r2;
+                slot[k + 1] = r1;
             }
         }
         __syncthreads();

@@ -1054,7 +1054,7 @@ __device__ void colored_sweep(const EngineArgs& A, const BlockCtx& B, unsigned l
                     acc = de <= 0;
                     if (!acc) {
                         const uint32_t thr = thr_row[min(de >> 1, kmax)];
-                        acc = (rng.next() < thr) || (thr == 0xFFFFFFFFu);
+                        acc = (rng.next_one() < thr) || (thr == 0xFFFFFFFFu);
                     }
                     if (acc) {
                         sp[i] = (int8_t)-s;

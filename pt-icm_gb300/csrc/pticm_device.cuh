@@ -148,6 +148,21 @@ struct ThreadRng12 {
         b2 = c;
         avail = 12;
     }
+    // The same stream one Philox block at a time, for threads that draw few
+    // words per sweep (the twelve-word refill would compute eight unused);
+    // a stream is drawn with next() or with next_one(), not both.
+    __device__ __forceinline__ uint32_t next_one() {
+        if (avail == 0) {
+            uint4 a = ctr;
+            a.w = calls++;
+            b0 = philox4x32_10(a, key);
+            avail = 4;
+        }
+        const uint32_t r = b0.x;
+        b0 = make_uint4(b0.y, b0.z, b0.w, 0u);
+        avail--;
+        return r;
+    }
     __device__ __forceinline__ uint32_t next() {
         if (avail == 0) refill();
         const uint32_t r = b0.x;

@@ -81,3 +81,54 @@ def test_reference_arm_other_ranks_exit_quietly():
     r = _run_bench(["--impl", "reference", "--steps", "1", "--warmup", "0", "--ref-pts", "2"], {"RANK": "1"})
     assert r.returncode == 0
     assert r.stdout.strip() == ""
+
+
+class _FakeStats:
+    def __init__(self, ms):
+        self.last_run_ms = ms
+
+
+class _FakeCtx:
+    """Stands in for pticm.Context in bench.phase_split: run() records the
+    phase mask, stats() reports a step time per mask, profile() returns
+    per-phase milliseconds summed over the profiled steps."""
+
+    NAMES = ("sweep", "barrier", "exchange", "icm", "total", "icm_diff", "icm_seed", "icm_union", "icm_flip",
+             "icm_energy", "x_draw", "x_levels", "x_apply", "x_shuffle", "uf_link0", "uf_compress", "uf_link1",
+             "uf_vote", "uf_outside", "uf_s_unions", "uf_size", "sweep_icm", "icm_pairs")
+
+    def __init__(self):
+        self.mask = 7
+        self.steps = 0
+        self.profiling = False
+
+    def run(self, steps, mask=7):
+        self.mask, self.steps = mask, steps
+
+    def stats(self):
+        us = {1: 10.0, 3: 12.0, 7: 20.0}[self.mask]
+        return _FakeStats(us * self.steps / 1e3), None, None
+
+    def set_profiling(self, on=True):
+        self.profiling = on
+
+    def profile(self):
+        mean = {k: 0.0 for k in self.NAMES}
+        mean.update(sweep=0.008 * self.steps, icm=0.004 * self.steps, uf_link0=0.001 * self.steps,
+                    icm_pairs=0.5 * self.steps)
+        return mean, dict(mean)
+
+
+def test_phase_split_units():
+    sys.path.insert(0, ROOT)
+    import bench
+    ctx = _FakeCtx()
+    out = bench.phase_split(ctx, 200, 100)
+    assert out["masked_us_per_step"] == pytest.approx({"sweep": 10.0, "sweep+exchange": 12.0, "all": 20.0})
+    assert out["us_per_step"]["sweep"][0] == pytest.approx(8.0)       # 0.008 ms per step
+    assert out["us_per_step"]["icm"][0] == pytest.approx(4.0)
+    assert out["icm_pairs_per_block"] == pytest.approx(0.5)
+    # per pair: 0.004 ms per step over 0.5 pairs per step
+    assert out["us_per_icm_pair"]["icm"] == pytest.approx(8.0)
+    assert out["us_per_icm_pair"]["uf_link0"] == pytest.approx(2.0)
+    assert "x_draw" not in out["us_per_step"] and not ctx.profiling
